@@ -1,0 +1,59 @@
+"""Python wrappers of the engine's level-2 kernels (GEMV, non-finite scan)."""
+
+from __future__ import annotations
+
+import torch
+
+from . import _ffi
+
+
+def as_device_f64(x: torch.Tensor) -> torch.Tensor:
+    """The tensor as a contiguous CUDA float64 tensor (copy only if needed)."""
+    if x.device.type != "cuda":
+        raise ValueError("lineax_gb300 operates on CUDA tensors; got a tensor on "
+                         f"{x.device}")
+    if x.dtype != torch.float64:
+        if x.is_complex():
+            raise ValueError("complex dtypes are not supported by lineax_gb300")
+        x = x.to(torch.float64)
+    return x.contiguous()
+
+
+def gemv(matrix: torch.Tensor, vector, trans: bool = False, alpha: float = 1.0,
+         beta: float = 0.0, out: torch.Tensor | None = None) -> torch.Tensor:
+    """alpha * op(matrix) @ vector (+ beta * out) on lxgb_gemv_f64.
+
+    `vector` may be 1-D (one vector) or 2-D (nvec, n) (several vectors).
+    Non-float64 operands are computed in float64 and cast back.
+    """
+    if isinstance(vector, (tuple, list, dict)):
+        raise ValueError("MatrixLinearOperator.mv expects a single 1-D tensor")
+    out_dtype = torch.promote_types(matrix.dtype, vector.dtype)
+    a = as_device_f64(matrix)
+    x = as_device_f64(vector)
+    m, n = a.shape
+    rows_out = n if trans else m
+    single = x.ndim == 1
+    xv = x.reshape(1, -1) if single else x
+    nvec = xv.shape[0]
+    if xv.shape[1] != (m if trans else n):
+        raise ValueError(f"gemv: vector of length {xv.shape[1]} for a {m}x{n} matrix")
+    if out is None:
+        y = torch.empty((nvec, rows_out), dtype=torch.float64, device=a.device)
+        beta = 0.0
+    else:
+        y = out.reshape(nvec, rows_out)
+    _ffi.call("lxgb_gemv_f64", m, n, _ffi.ptr(a), n, int(trans), nvec, _ffi.ptr(xv),
+              xv.shape[1], _ffi.ptr(y), rows_out, float(alpha), float(beta),
+              _ffi.stream_handle(a.device))
+    y = y[0] if single else y
+    return y if out_dtype == torch.float64 else y.to(out_dtype)
+
+
+def any_nonfinite(x: torch.Tensor) -> torch.Tensor:
+    """Device int32 flag (shape [1]): 1 if x holds a NaN or inf."""
+    flag = torch.empty(1, dtype=torch.int32, device=x.device)
+    xf = as_device_f64(x).reshape(-1)
+    _ffi.call("lxgb_nonfinite_f64", xf.numel(), _ffi.ptr(xf), _ffi.ptr(flag),
+              _ffi.stream_handle(x.device))
+    return flag

@@ -1,0 +1,109 @@
+"""ctypes binding of liblxgb.so (the C ABI declared in include/lxgb.h).
+
+This is the Python side of the drop-in boundary: every solver in this package
+reaches the GPU only through the functions bound here.  The library is loaded
+lazily on first use; if it is missing, or no CUDA device is visible, the call
+raises — there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import pathlib
+import threading
+
+_LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liblxgb.so"
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+c_i32 = ctypes.c_int32
+c_i64 = ctypes.c_int64
+c_f64 = ctypes.c_double
+c_p = ctypes.c_void_p
+
+# name -> (restype, argtypes); mirrors include/lxgb.h one to one.
+SIGNATURES: dict[str, tuple[object, list[object]]] = {
+    "lxgb_version": (ctypes.c_int, []),
+    "lxgb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "lxgb_last_error": (ctypes.c_char_p, []),
+    "lxgb_getrf_batched_f64": (ctypes.c_int, [c_i64, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_p]),
+    "lxgb_getrs_batched_f64": (
+        ctypes.c_int,
+        [c_i64, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_i64, c_i32, c_p],
+    ),
+    "lxgb_potrf_ragged_f64": (ctypes.c_int, [c_i64, c_i32, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_potrs_ragged_f64": (ctypes.c_int, [c_i64, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_posv_ragged_mixed_workspace_size": (c_i64, [c_i64, c_i32, c_i32]),
+    "lxgb_posv_ragged_mixed": (
+        ctypes.c_int,
+        [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
+         c_p, c_i64, c_p],
+    ),
+    "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
+    "lxgb_gemv_f64": (
+        ctypes.c_int,
+        [c_i64, c_i64, c_p, c_i64, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_f64, c_f64, c_p],
+    ),
+    "lxgb_nonfinite_f64": (ctypes.c_int, [c_i64, c_p, c_p, c_p]),
+    "lxgb_reduce_workspace_size": (c_i64, [c_i64]),
+    "lxgb_reduce_f64": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_diag_solve_f64": (ctypes.c_int, [c_i64, c_p, c_i64, c_p, c_p, c_i32, c_p]),
+}
+
+
+class LxgbError(RuntimeError):
+    """A library call failed with an argument or CUDA error (status >= 100)."""
+
+    def __init__(self, name: str, status: int, text: str):
+        super().__init__(f"{name} failed with status {status}: {text}")
+        self.status = status
+
+
+def lib_path() -> pathlib.Path:
+    return _LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load liblxgb.so and declare its signatures (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not _LIB_PATH.exists():
+            raise ImportError(
+                f"{_LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; "
+                "g.build()\"` (the solve engine has no CPU fallback)"
+            )
+        # torch first, so the process shares one CUDA runtime with it.
+        import torch  # noqa: F401
+
+        lib = ctypes.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def call(name: str, *args) -> int:
+    """Call an entry point; statuses 0..6 are returned, >= 100 raise."""
+    lib = load()
+    status = getattr(lib, name)(*args)
+    if status >= 100:
+        text = (lib.lxgb_last_error() or b"").decode()
+        raise LxgbError(name, status, text)
+    return status
+
+
+def ptr(t) -> int:
+    """Device pointer of a torch tensor (0 for None)."""
+    return 0 if t is None else t.data_ptr()
+
+
+def stream_handle(device=None) -> int:
+    import torch
+
+    return torch.cuda.current_stream(device).cuda_stream

@@ -1,0 +1,256 @@
+"""Linear operators over torch tensors (mirrors the in-scope part of
+lineax/_operator.py: MatrixLinearOperator :232-285, FunctionLinearOperator
+:664-732, IdentityLinearOperator, negation, the tag predicates :1587-1929,
+linearise :1206-1257 and materialise :1263-1388).
+
+Matrix-vector products of MatrixLinearOperator run on the engine's own GEMV
+kernel (lxgb_gemv_f64); FunctionLinearOperator calls the user's function.
+"""
+
+from __future__ import annotations
+
+import abc
+from typing import Callable
+
+import torch
+
+from . import _blas
+from ._structure import ShapeDtypeStruct, ravel, structure_of, tree_flatten, tree_size, unravel
+from ._tags import (
+    diagonal_tag,
+    lower_triangular_tag,
+    negative_semidefinite_tag,
+    positive_semidefinite_tag,
+    symmetric_tag,
+    transpose_tags,
+    tridiagonal_tag,
+    unit_diagonal_tag,
+    upper_triangular_tag,
+)
+
+
+def _frozenset(tags) -> frozenset:
+    if isinstance(tags, frozenset):
+        return tags
+    if isinstance(tags, (list, tuple, set)):
+        return frozenset(tags)
+    return frozenset([tags])
+
+
+class AbstractLinearOperator(abc.ABC):
+    """Abstract linear operator: `mv`, `as_matrix`, `transpose`, structures."""
+
+    tags: frozenset = frozenset()
+
+    @abc.abstractmethod
+    def mv(self, vector):
+        ...
+
+    @abc.abstractmethod
+    def as_matrix(self) -> torch.Tensor:
+        ...
+
+    @abc.abstractmethod
+    def transpose(self) -> "AbstractLinearOperator":
+        ...
+
+    @abc.abstractmethod
+    def in_structure(self):
+        ...
+
+    @abc.abstractmethod
+    def out_structure(self):
+        ...
+
+    @property
+    def T(self) -> "AbstractLinearOperator":
+        return self.transpose()
+
+    def in_size(self) -> int:
+        return tree_size(self.in_structure())
+
+    def out_size(self) -> int:
+        return tree_size(self.out_structure())
+
+    def __neg__(self) -> "AbstractLinearOperator":
+        return NegLinearOperator(self)
+
+
+class MatrixLinearOperator(AbstractLinearOperator):
+    """Wraps a 2-D tensor (lineax/_operator.py:232-285).  Vectors are 1-D."""
+
+    def __init__(self, matrix: torch.Tensor, tags=()):
+        if not isinstance(matrix, torch.Tensor) or matrix.ndim != 2:
+            raise ValueError("`MatrixLinearOperator(matrix=...)` should be 2-dimensional.")
+        if not torch.is_floating_point(matrix):
+            matrix = matrix.to(torch.get_default_dtype())
+        self.matrix = matrix
+        self.tags = _frozenset(tags)
+
+    def mv(self, vector):
+        return _blas.gemv(self.matrix, vector)
+
+    def as_matrix(self):
+        return self.matrix
+
+    def transpose(self):
+        if symmetric_tag in self.tags:
+            return self
+        return MatrixLinearOperator(self.matrix.T.contiguous(), transpose_tags(self.tags))
+
+    def in_structure(self):
+        return ShapeDtypeStruct((self.matrix.shape[1],), self.matrix.dtype)
+
+    def out_structure(self):
+        return ShapeDtypeStruct((self.matrix.shape[0],), self.matrix.dtype)
+
+
+class FunctionLinearOperator(AbstractLinearOperator):
+    """Wraps a linear function of a PyTree of tensors
+    (lineax/_operator.py:664-732).  `input_structure` is a PyTree of
+    ShapeDtypeStruct (or of example tensors)."""
+
+    def __init__(self, fn: Callable, input_structure, tags=(), output_structure=None):
+        self.fn = fn
+        self._in = structure_of(input_structure)
+        self._out = structure_of(output_structure) if output_structure is not None else None
+        self.tags = _frozenset(tags)
+
+    def mv(self, vector):
+        return self.fn(vector)
+
+    def as_matrix(self):
+        return materialise(self).matrix
+
+    def transpose(self):
+        if symmetric_tag in self.tags:
+            return self
+        return materialise(self).transpose()
+
+    def in_structure(self):
+        return self._in
+
+    def out_structure(self):
+        if self._out is None:
+            return self._in
+        return self._out
+
+
+class IdentityLinearOperator(AbstractLinearOperator):
+    """The identity on a structure (used as the default preconditioner)."""
+
+    tags = frozenset(
+        [symmetric_tag, diagonal_tag, unit_diagonal_tag, positive_semidefinite_tag]
+    )
+
+    def __init__(self, structure):
+        self._s = structure_of(structure)
+
+    def mv(self, vector):
+        return vector
+
+    def as_matrix(self):
+        leaves, _ = tree_flatten(self._s)
+        n = tree_size(self._s)
+        return torch.eye(n, dtype=leaves[0].dtype, device="cuda")
+
+    def transpose(self):
+        return self
+
+    def in_structure(self):
+        return self._s
+
+    def out_structure(self):
+        return self._s
+
+
+class NegLinearOperator(AbstractLinearOperator):
+    """-operator (used by Cholesky/CG for negative-definite operators)."""
+
+    def __init__(self, operator: AbstractLinearOperator):
+        self.operator = operator
+        t = operator.tags
+        swapped = set(t)
+        if positive_semidefinite_tag in t:
+            swapped.discard(positive_semidefinite_tag)
+            swapped.add(negative_semidefinite_tag)
+        elif negative_semidefinite_tag in t:
+            swapped.discard(negative_semidefinite_tag)
+            swapped.add(positive_semidefinite_tag)
+        swapped.discard(unit_diagonal_tag)
+        self.tags = frozenset(swapped)
+
+    def mv(self, vector):
+        out = self.operator.mv(vector)
+        leaves, td = tree_flatten(out)
+        from ._structure import tree_unflatten
+
+        return tree_unflatten(td, [-x for x in leaves])
+
+    def as_matrix(self):
+        return -self.operator.as_matrix()
+
+    def transpose(self):
+        return NegLinearOperator(self.operator.transpose())
+
+    def in_structure(self):
+        return self.operator.in_structure()
+
+    def out_structure(self):
+        return self.operator.out_structure()
+
+
+# -- tag predicates (lineax/_operator.py:1587-1929) -------------------------
+
+
+def is_symmetric(op) -> bool:
+    t = op.tags
+    return any(x in t for x in (symmetric_tag, positive_semidefinite_tag,
+                                negative_semidefinite_tag, diagonal_tag))  # real dtypes only
+
+
+def is_diagonal(op) -> bool:
+    return diagonal_tag in op.tags or (op.in_size() == 1 and op.out_size() == 1)
+
+
+def is_tridiagonal(op) -> bool:
+    return tridiagonal_tag in op.tags or diagonal_tag in op.tags
+
+
+def is_lower_triangular(op) -> bool:
+    return lower_triangular_tag in op.tags
+
+
+def is_upper_triangular(op) -> bool:
+    return upper_triangular_tag in op.tags
+
+
+def is_positive_semidefinite(op) -> bool:
+    return positive_semidefinite_tag in op.tags
+
+
+def is_negative_semidefinite(op) -> bool:
+    return negative_semidefinite_tag in op.tags
+
+
+def has_unit_diagonal(op) -> bool:
+    return unit_diagonal_tag in op.tags
+
+
+def linearise(op):
+    """Matrix and function operators are already linear (lineax/_operator.py:1206)."""
+    return op
+
+
+def materialise(op) -> MatrixLinearOperator:
+    """Turn an operator into a MatrixLinearOperator by applying it to the
+    columns of the identity (lineax/_operator.py:1369-1388)."""
+    if isinstance(op, MatrixLinearOperator):
+        return op
+    ins = op.in_structure()
+    leaves, _ = tree_flatten(ins)
+    dtype = leaves[0].dtype
+    n = tree_size(ins)
+    eye = torch.eye(n, dtype=dtype, device="cuda")
+    cols = [ravel(op.mv(unravel(eye[j], ins)), dtype) for j in range(n)]
+    return MatrixLinearOperator(torch.stack(cols, dim=1).contiguous(), op.tags)

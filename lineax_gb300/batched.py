@@ -1,0 +1,174 @@
+"""Batched and ragged solves: the vmapped and ragged forms of lineax's LU and
+Cholesky solves, and the mixed-precision SPD solve with FP64 refinement.
+
+* ``lu_solve_batched(A, b)`` — equal-size batch, FP64 LU (the form
+  ``jax.vmap(lambda A, b: lx.linear_solve(lx.MatrixLinearOperator(A), b,
+  lx.LU()).value)`` evaluates).
+* ``RaggedBatch`` — a ragged batch packed into one buffer with per-system
+  offsets (the layout of the C ABI), built once from lists of tensors.
+* ``cholesky_solve_ragged(batch)`` — plain FP64 potrf + potrs.
+* ``spd_solve_ragged_mixed(batch, tol)`` — FP32 factor + FP64 iterative
+  refinement to a normwise backward error <= tol, in one persistent launch.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+
+import torch
+
+from . import _dense, _ffi
+from ._blas import as_device_f64
+
+
+def lu_solve_batched(a: torch.Tensor, b: torch.Tensor, trans: int = 0):
+    """x[i] = A[i]^{-1} b[i] (or A[i]^{-T} b[i]) for a (batch, n, n) FP64 stack.
+    b is (batch, n) or (batch, nrhs, n).  Returns (x, info)."""
+    lu, piv, info = _dense.lu_factor_batched(a)
+    return _dense.lu_solve_batched(lu, piv, b, trans), info
+
+
+@dataclasses.dataclass
+class RaggedBatch:
+    """Systems of different orders packed back to back.
+
+    a: packed FP64 matrices (row-major), a_off[s] the start of system s.
+    b: packed right-hand sides, system s holds nrhs[s] vectors of length n[s]
+    from b_off[s].  n/nrhs/a_off/b_off live on the device; the host copies
+    (n_host, nrhs_host) size launches.
+    """
+
+    a: torch.Tensor
+    b: torch.Tensor
+    n: torch.Tensor
+    nrhs: torch.Tensor
+    a_off: torch.Tensor
+    b_off: torch.Tensor
+    n_host: list
+    nrhs_host: list
+    a_off_host: list
+    b_off_host: list
+
+    @property
+    def batch(self) -> int:
+        return len(self.n_host)
+
+    @property
+    def max_n(self) -> int:
+        return max(self.n_host) if self.n_host else 0
+
+    @property
+    def max_nrhs(self) -> int:
+        return max(self.nrhs_host) if self.nrhs_host else 0
+
+    @staticmethod
+    def layout(n_list, nrhs_list):
+        a_off, b_off, ao, bo = [], [], 0, 0
+        for n, k in zip(n_list, nrhs_list):
+            a_off.append(ao)
+            b_off.append(bo)
+            ao += n * n
+            bo += n * k
+        return a_off, b_off, ao, bo
+
+    @classmethod
+    def from_packed(cls, a, b, n_list, nrhs_list, device="cuda"):
+        """Wrap already-packed device buffers (a: Σn², b: Σn·nrhs)."""
+        a_off, b_off, ta, tb = cls.layout(n_list, nrhs_list)
+        if a.numel() != ta or b.numel() != tb:
+            raise ValueError("packed buffer sizes do not match the ragged layout")
+        meta_i32 = torch.tensor([list(n_list), list(nrhs_list)], dtype=torch.int32)
+        meta_i64 = torch.tensor([a_off, b_off], dtype=torch.int64)
+        meta_i32 = meta_i32.to(device)
+        meta_i64 = meta_i64.to(device)
+        return cls(a, b, meta_i32[0], meta_i32[1], meta_i64[0], meta_i64[1], list(n_list),
+                   list(nrhs_list), a_off, b_off)
+
+    @classmethod
+    def from_lists(cls, matrices, rhs, device="cuda"):
+        """matrices[s]: (n, n); rhs[s]: (n,) or (nrhs, n)."""
+        n_list = [int(m.shape[0]) for m in matrices]
+        nrhs_list = [1 if r.ndim == 1 else int(r.shape[0]) for r in rhs]
+        a = torch.cat([m.reshape(-1).to(torch.float64) for m in matrices]).to(device)
+        b = torch.cat([r.reshape(-1).to(torch.float64) for r in rhs]).to(device)
+        return cls.from_packed(a, b, n_list, nrhs_list, device)
+
+    def system_b(self, x: torch.Tensor, s: int) -> torch.Tensor:
+        """View of system s in a buffer with the layout of b: (nrhs, n)."""
+        n, k, o = self.n_host[s], self.nrhs_host[s], self.b_off_host[s]
+        return x[o : o + n * k].view(k, n)
+
+    def system_a(self, s: int) -> torch.Tensor:
+        n, o = self.n_host[s], self.a_off_host[s]
+        return self.a[o : o + n * n].view(n, n)
+
+
+def cholesky_factor_ragged(batch: RaggedBatch):
+    """Plain FP64 upper Cholesky of every system (a copy of batch.a).
+    Returns (factors packed like batch.a, info)."""
+    u = as_device_f64(batch.a).clone()
+    info = torch.empty(batch.batch, dtype=torch.int32, device=u.device)
+    _ffi.call("lxgb_potrf_ragged_f64", batch.batch, batch.max_n, _ffi.ptr(batch.n),
+              _ffi.ptr(batch.a_off), _ffi.ptr(u), _ffi.ptr(info), _ffi.stream_handle(u.device))
+    return u, info
+
+
+def cholesky_solve_ragged(batch: RaggedBatch, factors: torch.Tensor | None = None):
+    """Plain FP64 Cholesky solve of a ragged batch (the FP64 GPU baseline).
+    Returns (x packed like batch.b, info)."""
+    if factors is None:
+        factors, info = cholesky_factor_ragged(batch)
+    else:
+        info = torch.zeros(batch.batch, dtype=torch.int32, device=factors.device)
+    x = as_device_f64(batch.b).clone()
+    _ffi.call("lxgb_potrs_ragged_f64", batch.batch, batch.max_n, _ffi.ptr(batch.n),
+              _ffi.ptr(batch.nrhs), _ffi.ptr(batch.a_off), _ffi.ptr(factors),
+              _ffi.ptr(batch.b_off), _ffi.ptr(x), _ffi.stream_handle(x.device))
+    return x, info
+
+
+@dataclasses.dataclass
+class MixedResult:
+    x: torch.Tensor      # solutions, packed like batch.b
+    info: torch.Tensor   # per system: 0 ok, k+1 FP32 breakdown, -1 not converged
+    iters: torch.Tensor  # FP32 solves applied per system
+    berr: torch.Tensor   # largest normwise backward error per system
+
+
+class MixedWorkspace:
+    """Caller-side scratch of lxgb_posv_ragged_mixed, reusable across calls
+    (kept by the serving loop and by CUDA-graph captures)."""
+
+    def __init__(self, batch: int, max_n: int, max_nrhs: int, device="cuda"):
+        nbytes = _ffi.load().lxgb_posv_ragged_mixed_workspace_size(batch, max_n, max_nrhs)
+        self.nbytes = int(nbytes)
+        # 256-byte alignment: torch's caching allocator returns 512-byte aligned blocks.
+        self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        self.batch, self.max_n, self.max_nrhs = batch, max_n, max_nrhs
+
+    def fits(self, batch: int, max_n: int, max_nrhs: int) -> bool:
+        need = _ffi.load().lxgb_posv_ragged_mixed_workspace_size(batch, max_n, max_nrhs)
+        return need <= self.nbytes
+
+
+def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int = 10,
+                           workspace: MixedWorkspace | None = None,
+                           out: MixedResult | None = None) -> MixedResult:
+    """FP32-factor / FP64-refined solve of every SPD system of the batch."""
+    dev = batch.a.device
+    if workspace is None or not workspace.fits(batch.batch, batch.max_n, batch.max_nrhs):
+        workspace = MixedWorkspace(batch.batch, batch.max_n, batch.max_nrhs, dev)
+    if out is None:
+        out = MixedResult(
+            x=torch.empty_like(batch.b, dtype=torch.float64),
+            info=torch.empty(batch.batch, dtype=torch.int32, device=dev),
+            iters=torch.empty(batch.batch, dtype=torch.int32, device=dev),
+            berr=torch.empty(batch.batch, dtype=torch.float64, device=dev),
+        )
+    _ffi.call("lxgb_posv_ragged_mixed", batch.batch, batch.max_n, batch.max_nrhs,
+              _ffi.ptr(batch.n), _ffi.ptr(batch.nrhs), _ffi.ptr(batch.a_off),
+              _ffi.ptr(batch.a), _ffi.ptr(batch.b_off), _ffi.ptr(batch.b), _ffi.ptr(out.x),
+              float(tol), int(max_iter), _ffi.ptr(out.info), _ffi.ptr(out.iters),
+              _ffi.ptr(out.berr), _ffi.ptr(workspace.buf), workspace.nbytes,
+              _ffi.stream_handle(dev))
+    return out

@@ -1,0 +1,95 @@
+"""CPU: host-side logic of the lineax-style API (dispatch, structures, result
+codes, ragged layout) — nothing here launches a kernel."""
+
+import pytest
+import torch
+
+import lineax_gb300 as lx
+from lineax_gb300 import batched
+from lineax_gb300._structure import ravel, structure_of, tree_flatten, tree_unflatten, unravel
+
+
+def test_results_codes_match_lineax_order():
+    names = ["successful", "max_steps_reached", "singular", "breakdown", "stagnation",
+             "conlim", "nonfinite_input"]
+    for i, name in enumerate(names):
+        assert getattr(lx.RESULTS, name) == i
+        assert lx.RESULTS.name(i) == name
+    assert lx.RESULTS[lx.RESULTS.successful] == ""
+
+
+def _mat(tags=(), n=3):
+    return lx.MatrixLinearOperator(torch.eye(n, dtype=torch.float64), tags)
+
+
+@pytest.mark.parametrize(
+    "tags,expected",
+    [
+        ((), lx.LU),
+        (lx.lower_triangular_tag, lx.Triangular),
+        (lx.upper_triangular_tag, lx.Triangular),
+        (lx.positive_semidefinite_tag, lx.Cholesky),
+        (lx.negative_semidefinite_tag, lx.Cholesky),
+        (lx.diagonal_tag, lx.Diagonal),
+    ],
+)
+def test_auto_solver_dispatch_well_posed(tags, expected):
+    s = lx.AutoLinearSolver(well_posed=True).select_solver(_mat(tags))
+    assert isinstance(s, expected)
+
+
+def test_auto_solver_nonsquare():
+    op = lx.MatrixLinearOperator(torch.zeros(5, 3, dtype=torch.float64))
+    assert lx.AutoLinearSolver(well_posed=None)._select_solver(op) == "qr_token"
+    with pytest.raises(ValueError):
+        lx.AutoLinearSolver(well_posed=True).select_solver(op)
+
+
+def test_transpose_tags():
+    t = lx.transpose_tags(frozenset([lx.lower_triangular_tag, lx.unit_diagonal_tag]))
+    assert t == frozenset([lx.upper_triangular_tag, lx.unit_diagonal_tag])
+    sym = frozenset([lx.symmetric_tag, lx.lower_triangular_tag])
+    assert lx.transpose_tags(sym) == sym
+
+
+def test_raw_array_rejected():
+    with pytest.raises(ValueError):
+        lx.linear_solve(torch.eye(2), torch.ones(2))
+
+
+def test_structure_mismatch_rejected():
+    op = _mat(n=3)
+    with pytest.raises(ValueError):
+        lx.linear_solve(op, torch.ones(4, dtype=torch.float64))
+
+
+def test_solver_init_checks():
+    with pytest.raises(ValueError):
+        lx.Cholesky().init(_mat(), {})
+    with pytest.raises(ValueError):
+        lx.Triangular().init(_mat(), {})
+    with pytest.raises(ValueError):
+        lx.LU().init(lx.MatrixLinearOperator(torch.zeros(2, 3, dtype=torch.float64)), {})
+
+
+def test_pytree_ravel_roundtrip():
+    tree = {"b": torch.arange(3.0), "a": (torch.tensor(1.0), torch.arange(4.0).reshape(2, 2))}
+    leaves, td = tree_flatten(tree)
+    assert [tuple(x.shape) for x in leaves] == [(), (2, 2), (3,)]  # sorted dict keys
+    flat = ravel(tree, torch.float64)
+    assert flat.tolist() == [1.0, 0, 1, 2, 3, 0, 1, 2]
+    back = unravel(flat, structure_of(tree))
+    assert torch.equal(back["b"], tree["b"].double())
+    assert tree_unflatten(td, leaves)["a"][0] is leaves[0]
+
+
+def test_ragged_layout_offsets():
+    a_off, b_off, ta, tb = batched.RaggedBatch.layout([2, 3], [1, 2])
+    assert a_off == [0, 4] and b_off == [0, 2] and ta == 13 and tb == 8
+
+
+def test_identity_operator_short_circuit():
+    op = lx.IdentityLinearOperator(torch.zeros(3, dtype=torch.float64))
+    v = torch.arange(3.0, dtype=torch.float64)
+    sol = lx.linear_solve(op, v)
+    assert sol.value is v and sol.result == lx.RESULTS.successful

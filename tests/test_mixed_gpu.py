@@ -1,0 +1,105 @@
+"""GPU parity: ragged batched Cholesky, plain FP64 and mixed precision
+(FP32 factor + FP64 refinement), against the SciPy oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+from lineax_gb300 import batched
+from oracle import dense
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def make_ragged(rng, ns, ks):
+    mats, rhs = [], []
+    for n, k in zip(ns, ks):
+        g = rng.standard_normal((n, n))
+        mats.append(g @ g.T / n + 1e-2 * np.eye(n))
+        rhs.append(rng.standard_normal((k, n)))
+    return mats, rhs
+
+
+def to_batch(mats, rhs, dev):
+    return batched.RaggedBatch.from_lists([torch.tensor(m) for m in mats],
+                                          [torch.tensor(r) for r in rhs], device=dev)
+
+
+@pytest.mark.parametrize("ns", [[16, 17, 33], [64, 128, 160], [161, 224, 225, 300, 512]])
+def test_ragged_potrf_potrs_f64(dev, ns):
+    rng = np.random.default_rng(sum(ns))
+    ks = [1 + (i % 3) for i in range(len(ns))]
+    mats, rhs = make_ragged(rng, ns, ks)
+    rb = to_batch(mats, rhs, dev)
+    u, info = batched.cholesky_factor_ragged(rb)
+    assert int(info.abs().sum()) == 0
+    x, _ = batched.cholesky_solve_ragged(rb, u)
+    for s, (m, r) in enumerate(zip(mats, rhs)):
+        us = u[rb.a_off_host[s]: rb.a_off_host[s] + ns[s] ** 2].view(ns[s], ns[s]).cpu().numpy()
+        np.testing.assert_allclose(us, dense.cho_factor_upper(m), rtol=1e-9, atol=1e-11)
+        xs = rb.system_b(x, s).cpu().numpy()
+        for k in range(ks[s]):
+            assert dense.backward_error(m, xs[k], r[k]) <= TOL
+
+
+@pytest.mark.parametrize("ns", [[16, 17, 40, 100], [200, 224, 225, 256], [300, 400, 512]])
+def test_mixed_reaches_fp64_backward_error(dev, ns):
+    rng = np.random.default_rng(len(ns) * 1000 + ns[0])
+    ks = [1 + (3 * i) % 8 for i in range(len(ns))]
+    mats, rhs = make_ragged(rng, ns, ks)
+    rb = to_batch(mats, rhs, dev)
+    res = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    info = res.info.cpu().numpy()
+    iters = res.iters.cpu().numpy()
+    berr = res.berr.cpu().numpy()
+    assert (info == 0).all(), info
+    assert (iters >= 2).all() and (iters <= 10).all(), iters
+    for s, (m, r) in enumerate(zip(mats, rhs)):
+        xs = rb.system_b(res.x, s).cpu().numpy()
+        worst = 0.0
+        for k in range(ks[s]):
+            ref = dense.cholesky_linear_solve(m, r[k])
+            be = dense.backward_error(m, xs[k], r[k])
+            worst = max(worst, be)
+            assert be <= TOL
+            assert dense.forward_error(xs[k], ref) <= 1e-9
+        assert berr[s] <= TOL and berr[s] >= 0.0
+        assert worst <= 10 * max(berr[s], 1e-17)
+
+
+def test_mixed_many_rhs_chunks(dev):
+    rng = np.random.default_rng(3)
+    mats, rhs = make_ragged(rng, [50, 250], [20, 17])
+    rb = to_batch(mats, rhs, dev)
+    res = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    assert (res.info.cpu().numpy() == 0).all()
+    for s, (m, r) in enumerate(zip(mats, rhs)):
+        xs = rb.system_b(res.x, s).cpu().numpy()
+        for k in range(r.shape[0]):
+            assert dense.backward_error(m, xs[k], r[k]) <= TOL
+
+
+def test_mixed_not_spd_reports_breakdown(dev):
+    rng = np.random.default_rng(4)
+    good = make_ragged(rng, [30], [1])
+    bad = np.diag(np.concatenate([np.ones(10), [-1.0], np.ones(9)]))
+    mats = [good[0][0], bad]
+    rhs = [good[1][0], rng.standard_normal((1, 20))]
+    rb = to_batch(mats, rhs, dev)
+    res = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    info = res.info.cpu().numpy()
+    assert info[0] == 0 and info[1] == 11
+    assert np.isnan(rb.system_b(res.x, 1).cpu().numpy()).all()
+
+
+def test_mixed_result_independent_of_batch_mix(dev):
+    """A system's result is the same alone and inside a larger ragged mix."""
+    rng = np.random.default_rng(6)
+    mats, rhs = make_ragged(rng, [37, 190, 300, 64], [2, 1, 3, 1])
+    rb = to_batch(mats, rhs, dev)
+    res_all = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    for s in range(len(mats)):
+        alone = to_batch([mats[s]], [rhs[s]], dev)
+        res1 = batched.spd_solve_ragged_mixed(alone, tol=TOL)
+        assert torch.equal(rb.system_b(res_all.x, s), alone.system_b(res1.x, 0))

@@ -1,0 +1,92 @@
+"""CPU: the oracle against the reference's own known answers (tests/golden)
+and the C getf2 twin against SciPy's LAPACK."""
+
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+from oracle import dense, krylov
+from oracle.build import getf2_batched
+
+GOLD = json.loads((pathlib.Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+
+
+@pytest.mark.parametrize("name", ["pytree_2x2", "mixed_dtypes_2x2"])
+def test_oracle_lu_qr_kats(name):
+    k = GOLD[name]
+    a, b, x = np.array(k["matrix"]), np.array(k["vector"]), np.array(k["solution"])
+    np.testing.assert_allclose(dense.lu_linear_solve(a, b), x, rtol=1e-14)
+    np.testing.assert_allclose(dense.qr_linear_solve(a, b), x, rtol=1e-14)
+
+
+def test_oracle_triangular_kat():
+    k = GOLD["triangular_2x2"]
+    a, b, x = np.array(k["matrix"]), np.array(k["vector"]), np.array(k["solution"])
+    np.testing.assert_allclose(dense.triangular_solve(a, b, lower=True, unit_diagonal=False), x)
+
+
+def test_oracle_gmres_reports_failure_on_reference_4x4():
+    k = GOLD["gmres_fails_4x4"]
+    a = np.array(k["matrix"])
+    b = a @ np.array(k["true_x"])
+    s = k["solver"]
+    x, result, _ = krylov.gmres(lambda v: a @ v, b, rtol=s["rtol"], atol=s["atol"],
+                                restart=s["restart"])
+    assert krylov.finalize_result(x, result, b) != krylov.SUCCESSFUL
+
+
+def test_oracle_nonfinite_input_kat():
+    k = GOLD["nonfinite_input"]
+    d = np.array(k["diagonal"])
+    for v in k["vectors"]:
+        v = np.array(v)
+        x = v / d
+        assert krylov.finalize_result(x, krylov.SUCCESSFUL, v) == 6
+
+
+def test_getf2_twin_matches_lapack_pivots():
+    rng = np.random.default_rng(1)
+    for n in (1, 2, 7, 33, 128, 200):
+        a = rng.standard_normal((n, n))
+        lu, piv, info = getf2_batched(a)
+        lu_ref, piv_ref = dense.lu_factor(a)
+        assert info[0] == 0
+        np.testing.assert_array_equal(piv[0], piv_ref)
+        np.testing.assert_allclose(lu[0], lu_ref, rtol=0, atol=1e-11 * max(1, n))
+
+
+def test_getf2_twin_zero_pivot_info():
+    a = np.array([[0.0, 1.0], [0.0, 2.0]])
+    _, piv, info = getf2_batched(a)
+    assert info[0] == 1  # first column all zero: LAPACK reports info = 1
+
+
+def test_oracle_cg_poisson_converges():
+    n = 50
+    p = -2 * np.eye(n) + np.eye(n, k=1) + np.eye(n, k=-1)
+    a = -p  # positive definite
+    b = np.random.default_rng(0).standard_normal(n)
+    x, result, steps = krylov.cg(lambda v: a @ v, b, rtol=1e-10, atol=1e-10)
+    assert result == krylov.SUCCESSFUL and steps <= n + 5
+    assert dense.backward_error(a, x, b) < 1e-12
+
+
+def test_oracle_gmres_dense_converges():
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((40, 40))
+    xt = rng.standard_normal(40)
+    b = a @ xt
+    x, result, _ = krylov.gmres(lambda v: a @ v, b, rtol=1e-10, atol=1e-10, restart=40)
+    assert result == krylov.SUCCESSFUL
+    np.testing.assert_allclose(x, xt, rtol=1e-8, atol=1e-8)
+
+
+def test_oracle_cg_max_steps_only_poisson():
+    """tests/test_solve.py::test_iterative_solver_max_steps_only, CG leg."""
+    n = 100
+    p = -2 * np.eye(n) + np.eye(n, k=1) + np.eye(n, k=-1)
+    b = np.random.default_rng(0).standard_normal(n)
+    x, result, steps = krylov.cg(lambda v: p @ v, b, rtol=0.0, atol=0.0, max_steps=2, nsd=True)
+    assert steps == 2 and result == krylov.SUCCESSFUL
