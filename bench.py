@@ -1,0 +1,417 @@
+"""Benchmark of the solve engine on the ragged batched Cholesky workload.
+
+Workload (one "step"): 4096 SPD systems, n log-uniform in [16, 512],
+A = G Gᵀ/n + 1e-2·I, 1..8 right-hand sides each, solved to a normwise backward
+error <= 1e-12 by the mixed-precision path (FP32 factor, FP64 refinement) in
+one persistent launch.  Metric: solves/s (systems with all their right-hand
+sides solved per second), with per-step p50/p99 latency and, beside it, the
+plain FP64 GPU path (FP64 potrf + potrs) on the same inputs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path on the host cores: lineax's
+Cholesky solve lowers to LAPACK potrf/potrs (lineax/_solver/cholesky.py:60,74),
+which JAX's CPU backend takes from SciPy, so SciPy's FP64 cho_factor/cho_solve
+run in a spawn-started process pool over a sample of the same workload.
+Under torchrun every rank solves its own 4096 systems (weak scaling, no
+collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TOL = 1e-12
+COUNT = 4096
+SEED = 0
+METRIC = "solves/s and p50/p99 latency at <=1e-12 backward error vs plain FP64 GPU"
+UNIT = "solves/s"
+WORKLOAD = "ragged_spd_cholesky_4096"
+
+
+# ---------------------------------------------------------------------------
+# CPU side (reference arm and cpu_baseline): SciPy LAPACK in worker processes
+# ---------------------------------------------------------------------------
+_W = {}
+
+
+def _cpu_worker_init(seed, picks):
+    import numpy as np
+
+    from lineax_gb300 import workloads
+
+    n, k = workloads.ragged_spd_sizes(seed, COUNT)
+    _W["systems"] = [workloads.spd_system(seed, s, n[s], k[s]) for s in picks]
+    _W["np"] = np
+
+
+def _cpu_worker_solve(_):
+    import scipy.linalg as sl
+
+    worst = 0.0
+    for a, b in _W["systems"]:
+        c = sl.cho_factor(a, lower=False, check_finite=False)
+        x = sl.cho_solve(c, b.T, check_finite=False)
+        worst = max(worst, float(abs(x[0, 0])))
+    return len(_W["systems"]), worst
+
+
+def _cpu_pool(seed, sample, cores):
+    """A spawn pool whose workers hold disjoint parts of `sample`."""
+    import multiprocessing as mp
+
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    ctx = mp.get_context("spawn")
+    parts = [sample[i::cores] for i in range(cores)]
+    pools = [ctx.Pool(1, initializer=_cpu_worker_init, initargs=(seed, p)) for p in parts]
+    return pools
+
+
+def _cpu_step(pools):
+    rs = [p.apply_async(_cpu_worker_solve, (0,)) for p in pools]
+    return sum(r.get()[0] for r in rs)
+
+
+def cpu_sample(seed, size):
+    import numpy as np
+
+    rng = np.random.default_rng([seed, 77])
+    return sorted(rng.choice(COUNT, size=size, replace=False).tolist())
+
+
+def run_cpu_baseline(seed, size=1024, min_seconds=10.0, cores=None):
+    """Solve a random sample of the workload repeatedly for >= min_seconds."""
+    cores = cores or len(os.sched_getaffinity(0))
+    pools = _cpu_pool(seed, cpu_sample(seed, size), cores)
+    try:
+        _cpu_step(pools)  # warm-up (imports, first-touch)
+        done, t0 = 0, time.perf_counter()
+        while True:
+            done += _cpu_step(pools)
+            el = time.perf_counter() - t0
+            if el >= min_seconds:
+                break
+    finally:
+        for p in pools:
+            p.terminate()
+    return {
+        "value": done / el,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{size} systems drawn uniformly from the {COUNT}-system workload, "
+                  f"solved repeatedly for {el:.1f} s with SciPy LAPACK FP64 "
+                  "cho_factor(lower=False)+cho_solve, one process per core",
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    size = 1024
+    pools = _cpu_pool(SEED, cpu_sample(SEED, size), cores)
+    times = []
+    try:
+        for _ in range(args.warmup):
+            _cpu_step(pools)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _cpu_step(pools)
+            times.append(time.perf_counter() - t0)
+    finally:
+        for p in pools:
+            p.terminate()
+    total = sum(times)
+    value = size * len(times) / total
+    lat = sorted(t * 1e3 for t in times)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": WORKLOAD, "systems": COUNT, "n": "log-uniform [16,512]",
+                   "nrhs": "1..8", "tol": TOL, "step": f"{size}-system sample"},
+        "latency_ms": {"p50": _pct(lat, 50), "p99": _pct(lat, 99)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{size} of {COUNT} systems per step, SciPy LAPACK FP64 "
+                                   "potrf/potrs (the routines lineax's Cholesky reaches on "
+                                   "JAX-CPU), one process per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+def _pct(sorted_vals, p):
+    if not sorted_vals:
+        return None
+    i = min(len(sorted_vals) - 1, max(0, int(round(p / 100 * (len(sorted_vals) - 1)))))
+    return sorted_vals[i]
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags)
+                          if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from lineax_gb300 import batched, workloads
+    from oracle import dense
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # cpu baseline first (spawned workers, rank 0 only)
+    cpu = run_cpu_baseline(SEED) if (rank == 0 and not args.no_cpu) else None
+
+    wl = workloads.ragged_spd(SEED + rank, COUNT)
+    a_host = torch.from_numpy(wl.a).pin_memory()
+    b_host = torch.from_numpy(wl.b).pin_memory()
+    rb = batched.RaggedBatch.from_packed(a_host.to(dev), b_host.to(dev), wl.n, wl.nrhs, dev)
+    ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, dev)
+    out = batched.spd_solve_ragged_mixed(rb, TOL, workspace=ws)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        batched.spd_solve_ragged_mixed(rb, TOL, workspace=ws, out=out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        t_all0 = torch.cuda.Event(enable_timing=True)
+        t_all1 = torch.cuda.Event(enable_timing=True)
+        t_all0.record(stream)
+        for s0, s1 in ev:
+            s0.record(stream)
+            step()
+            s1.record(stream)
+        t_all1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    total_ms = t_all0.elapsed_time(t_all1)
+    per_step = sorted(s0.elapsed_time(s1) for s0, s1 in ev)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt)
+
+    # correctness of the timed results
+    info = out.info.cpu().numpy()
+    berr = out.berr.cpu().numpy()
+    iters = out.iters.cpu().numpy()
+    ok = bool((info == 0).all() and (berr <= TOL).all())
+    x_host = out.x.cpu().numpy()
+    check = []
+    for s in (0, len(wl.n) // 2, len(wl.n) - 1):
+        n, k = wl.n[s], wl.nrhs[s]
+        a_s = rb.system_a(s).cpu().numpy()
+        xs = x_host[rb.b_off_host[s]: rb.b_off_host[s] + n * k].reshape(k, n)
+        bs = wl.b[rb.b_off_host[s]: rb.b_off_host[s] + n * k].reshape(k, n)
+        check.append(max(dense.backward_error(a_s, xs[j], bs[j]) for j in range(k)))
+    ok = ok and max(check) <= TOL
+
+    # plain FP64 GPU path on the same inputs (factor + solve)
+    fp64_steps = max(2, min(args.steps, 5))
+    u, _ = batched.cholesky_factor_ragged(rb)
+    batched.cholesky_solve_ragged(rb, u)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(fp64_steps):
+        u, finfo = batched.cholesky_factor_ragged(rb)
+        x64, _ = batched.cholesky_solve_ragged(rb, u)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = f0.elapsed_time(f1) / fp64_steps
+    fp64_ok = bool((finfo.cpu().numpy() == 0).all())
+    del u, x64
+
+    # end to end through the public host-buffer API
+    hs = batched.HostRaggedSPDSolver(wl.n, wl.nrhs, TOL, device=dev)
+    x_h = torch.empty(hs.out.x.numel(), dtype=torch.float64).pin_memory()
+    i_h = torch.empty(rb.batch, dtype=torch.int32).pin_memory()
+    it_h = torch.empty(rb.batch, dtype=torch.int32).pin_memory()
+    be_h = torch.empty(rb.batch, dtype=torch.float64).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        hs(a_host, b_host, x_h, i_h, it_h, be_h)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        hs(a_host, b_host, x_h, i_h, it_h, be_h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_ok = bool((i_h.numpy() == 0).all() and (be_h.numpy() <= TOL).all())
+
+    if rank != 0:
+        return
+    ns = np.array(wl.n, dtype=np.float64)
+    ks = np.array(wl.nrhs, dtype=np.float64)
+    it = iters.astype(np.float64)
+    hbm_bytes = float((8 * ns * ns).sum() + (16 * ns * ks).sum())  # A read once, b in, x out
+    fp32_flops = float((ns ** 3 / 3).sum() + (4 * ns * ns * ks * it).sum())
+    fp64_flops = float((2 * ns * ns * ks * it).sum())
+    ms = total_ms / args.steps
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = hbm_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": COUNT * world / (ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 factor + f64 refinement",
+        "data": "synthetic (seeded numpy PCG64, per-system streams)",
+        "config": {
+            "workload": WORKLOAD, "systems_per_gpu": COUNT, "n": "log-uniform [16,512]",
+            "nrhs": "1..8", "A": "G G^T/n + 1e-2 I", "tol": TOL,
+            "l2": "inputs larger than L2 (%.2f GB of matrices per step)" % (8 * (ns * ns).sum() / 1e9),
+            "parallelism": f"replicas x{world}",
+        },
+        "latency_ms": {"p50": _pct(per_step, 50), "p99": _pct(per_step, 99)},
+        "correct": {"all_berr_le_tol": ok, "max_berr": float(berr.max()),
+                    "iters_mean": float(it.mean()), "iters_max": int(it.max())},
+        "fp64_plain_gpu": {"value": COUNT / (fp64_ms * 1e-3), "unit": UNIT,
+                           "ms_per_step": fp64_ms, "info_ok": fp64_ok,
+                           "speedup_of_mixed": fp64_ms / ms},
+        "e2e": {"value": COUNT / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": hs.h2d_bytes, "d2h_bytes_per_step": hs.d2h_bytes,
+                "ok": e2e_ok},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {
+            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None,
+            "kernel": "posv_mixed_kernel",
+            "note": "HBM roofline of the algorithmic bytes (A read once, b, x); the kernel is "
+                    "issue-bound on FP64 (residual) and FP32 (factor), see compute",
+            "compute": {"fp32_flops": fp32_flops, "fp64_flops": fp64_flops,
+                        "fp32_tflops": fp32_flops / (ms * 1e-3) / 1e12,
+                        "fp64_tflops": fp64_flops / (ms * 1e-3) / 1e12},
+        },
+        "clocks": clk.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    global COUNT
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline measurement")
+    p.add_argument("--systems", type=int, default=COUNT,
+                   help="systems per GPU (smaller values are for profiling runs only)")
+    args = p.parse_args()
+    COUNT = args.systems
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -172,3 +172,41 @@ def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int
               _ffi.ptr(out.berr), _ffi.ptr(workspace.buf), workspace.nbytes,
               _ffi.stream_handle(dev))
     return out
+
+
+class HostRaggedSPDSolver:
+    """Solve ragged SPD batches whose data lives in host memory.
+
+    Device buffers, metadata and the workspace are allocated once for a fixed
+    layout (n_list, nrhs_list); each call copies the matrices and right-hand
+    sides in from (pinned) host tensors on the current stream, runs the
+    mixed-precision solve, and copies solutions and per-system status back.
+    """
+
+    def __init__(self, n_list, nrhs_list, tol: float = 1e-12, max_iter: int = 10,
+                 device="cuda"):
+        a_off, b_off, ta, tb = RaggedBatch.layout(n_list, nrhs_list)
+        self.a_dev = torch.empty(ta, dtype=torch.float64, device=device)
+        self.b_dev = torch.empty(tb, dtype=torch.float64, device=device)
+        self.batch = RaggedBatch.from_packed(self.a_dev, self.b_dev, n_list, nrhs_list, device)
+        self.ws = MixedWorkspace(self.batch.batch, self.batch.max_n, self.batch.max_nrhs, device)
+        nb = self.batch.batch
+        self.out = MixedResult(
+            x=torch.empty(tb, dtype=torch.float64, device=device),
+            info=torch.empty(nb, dtype=torch.int32, device=device),
+            iters=torch.empty(nb, dtype=torch.int32, device=device),
+            berr=torch.empty(nb, dtype=torch.float64, device=device),
+        )
+        self.tol, self.max_iter = tol, max_iter
+        self.h2d_bytes = (ta + tb) * 8
+        self.d2h_bytes = tb * 8 + nb * (4 + 4 + 8)
+
+    def __call__(self, a_host: torch.Tensor, b_host: torch.Tensor, x_host: torch.Tensor,
+                 info_host: torch.Tensor, iters_host: torch.Tensor, berr_host: torch.Tensor):
+        self.a_dev.copy_(a_host, non_blocking=True)
+        self.b_dev.copy_(b_host, non_blocking=True)
+        spd_solve_ragged_mixed(self.batch, self.tol, self.max_iter, self.ws, self.out)
+        x_host.copy_(self.out.x, non_blocking=True)
+        info_host.copy_(self.out.info, non_blocking=True)
+        iters_host.copy_(self.out.iters, non_blocking=True)
+        berr_host.copy_(self.out.berr, non_blocking=True)
