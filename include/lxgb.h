@@ -130,6 +130,32 @@ int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
                            int32_t* iters, double* berr, void* work,
                            int64_t work_bytes, void* stream);
 
+/* Allocation-free form of lxgb_posv_ragged_mixed (no counterpart in the
+ * reference).  It is for callers that cannot allocate device memory when they
+ * solve — an XLA/JAX FFI handler, whose device memory belongs to XLA and where
+ * a cudaMalloc can synchronise the device or break a graph capture, or a
+ * serving / real-time loop that forbids allocation after start-up.  Arguments
+ * and results are those of lxgb_posv_ragged_mixed without `work`: the scratch
+ * is a fixed array of LXGB_POSV_NOALLOC_SCRATCH_BYTES (16 MiB + 256 B) inside
+ * the library, which every GPU that loads the library holds until the process
+ * exits.  Limits: max_n <= 2048 (larger is rejected with LXGB_INVALID_ARG);
+ * systems with n > 224 factor in 16 MiB / (4·max_n²) slices, so fewer CTAs run
+ * them than in the workspace form (at max_n = 512, 16 at a time).
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call uses the same array and leaves its contents behind (the call
+ * clears the work-queue counter itself): calls that overlap on the GPU — on
+ * two streams, or from two threads — race and must be serialised by the
+ * caller.  Calls nothing that allocates. */
+#define LXGB_POSV_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u + 256u)
+int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n,
+                                   int32_t max_nrhs, const int32_t* n,
+                                   const int32_t* nrhs, const int64_t* a_off,
+                                   const double* a, const int64_t* b_off,
+                                   const double* b, double* x, double tol,
+                                   int32_t max_iter, int32_t* info,
+                                   int32_t* iters, double* berr, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */

@@ -39,6 +39,11 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
          c_p, c_i64, c_p],
     ),
+    "lxgb_posv_ragged_mixed_noalloc": (
+        ctypes.c_int,
+        [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
+         c_p],
+    ),
     "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
     "lxgb_gemv_f64": (
         ctypes.c_int,

@@ -462,3 +462,93 @@ extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_
       queue, factor_ws);
   return check_launch("posv_mixed");
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of lxgb_posv_ragged_mixed.
+//
+// Some callers cannot allocate device memory at the moment they need a solve:
+// an XLA/JAX FFI handler owns no allocator of its own (device memory belongs to
+// XLA, and a cudaMalloc inside the handler can synchronise the device or break
+// a CUDA-graph capture XLA is recording), and a serving loop or real-time
+// controller may forbid allocation once it has started.  For them the scratch
+// of the mixed solve (work-queue counter + FP32 factors of systems too large for
+// shared memory) lives in the fixed array below, which every GPU that loads this
+// library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace lxgb {
+
+static __device__ __align__(256) unsigned char g_posv_noalloc_scratch[LXGB_POSV_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 64;
+static void* g_noalloc_addr[kNoallocMaxDevices] = {nullptr};
+static std::mutex g_noalloc_mu;
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is not a device address).
+static int noalloc_scratch_address(void** out) {
+  int dev = -1;
+  LXGB_CUDA_TRY(cudaGetDevice(&dev), "posv_mixed_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNoallocMaxDevices) {
+    set_last_error("posv_mixed_noalloc: device ordinal %d out of range", dev);
+    return LXGB_INVALID_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    LXGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_posv_noalloc_scratch),
+                  "posv_mixed_noalloc: cudaGetSymbolAddress");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return LXGB_SUCCESSFUL;
+}
+
+}  // namespace lxgb
+
+extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int32_t max_nrhs,
+                                              const int32_t* n, const int32_t* nrhs,
+                                              const int64_t* a_off, const double* a,
+                                              const int64_t* b_off, const double* b, double* x,
+                                              double tol, int32_t max_iter, int32_t* info,
+                                              int32_t* iters, double* berr, void* stream) {
+  LXGB_REQUIRE(batch >= 0 && max_n >= 0 && max_nrhs >= 0, "posv_mixed_noalloc: negative size");
+  if (batch == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(batch < (1LL << 31), "posv_mixed_noalloc: batch too large");
+  LXGB_REQUIRE(n && nrhs && a_off && a && b_off && b && x && info && iters && berr,
+               "posv_mixed_noalloc: null pointer");
+  LXGB_REQUIRE(max_iter >= 1, "posv_mixed_noalloc: max_iter must be >= 1");
+  LXGB_REQUIRE(max_n <= kMixedMaxN,
+               "posv_mixed_noalloc: max_n above 2048 (its FP32 factor exceeds the fixed scratch)");
+  // Grid: one FP32 factor slice per CTA for systems above the shared-memory
+  // size, as many slices as the fixed scratch holds.
+  int64_t grid = sm_count();
+  if (batch < grid) grid = batch;
+  if (max_n > kCholSmemMaxF32) {
+    const int64_t slice = (int64_t)max_n * max_n * (int64_t)sizeof(float);
+    const int64_t slices = (int64_t)(LXGB_POSV_NOALLOC_SCRATCH_BYTES - kQueueHeader) / slice;
+    if (slices < 1) {
+      set_last_error("posv_mixed_noalloc: max_n=%d needs %lld bytes of scratch, limit %lld", max_n,
+                     (long long)(slice + kQueueHeader),
+                     (long long)LXGB_POSV_NOALLOC_SCRATCH_BYTES);
+      return LXGB_INVALID_ARG;
+    }
+    if (slices < grid) grid = slices;
+  }
+  void* scratch = nullptr;
+  int rc = noalloc_scratch_address(&scratch);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  int* queue = reinterpret_cast<int*>(scratch);
+  float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + kQueueHeader);
+  reset_queue_kernel<<<1, 1, 0, st>>>(queue);  // the array keeps the previous call's counter
+  const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
+  LXGB_CUDA_TRY(cudaFuncSetAttribute(posv_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem),
+                "posv_mixed_noalloc: set smem");
+  posv_mixed_kernel<<<(unsigned)grid, kCholThreads, smem, st>>>(
+      batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
+      queue, factor_ws);
+  return check_launch("posv_mixed_noalloc");
+}
