@@ -157,6 +157,123 @@ int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n,
                                    int32_t* iters, double* berr, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Householder QR.                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* QR of a tall m×n FP64 matrix M (n <= m) by Householder reflectors.  Input:
+ * a_layout 0 — `a` is M itself, row-major m×n; a_layout 1 — `a` already holds
+ * Mᵀ (n×m row-major, e.g. a wide operator that lineax transposes).  Output in
+ * the raw layout of jnp.linalg.qr(M, mode="raw"): h = n×m row-major with R on
+ * and above the diagonal of hᵀ and the reflectors v_k (v_k[k] = 1 implied)
+ * below it, tau[n] the reflector scalars (LAPACK geqrf/larfg rules), and
+ * t[lxgb_geqrf_t_elems(n)] the compact-WY T matrices of each 32-reflector
+ * panel (used by lxgb_ormqr_f64).  `work`: lxgb_geqrf_workspace_size(m, n)
+ * bytes.  Replaces jnp.linalg.qr(matrix, mode="raw") at
+ * lineax/_solver/qr.py:62. */
+int64_t lxgb_geqrf_t_elems(int64_t n);
+int64_t lxgb_geqrf_workspace_size(int64_t m, int64_t n);
+int lxgb_geqrf_f64(int64_t m, int64_t n, const double* a, int32_t a_layout,
+                   double* h, double* tau, double* t, void* work,
+                   int64_t work_bytes, void* stream);
+
+/* Apply Qᵀ (trans 1) or Q (trans 0) of a factor from lxgb_geqrf_f64 to nrhs
+ * vectors of length m stored back to back in c (in place).  `work`:
+ * lxgb_ormqr_workspace_size(m, nrhs) bytes.  Replaces lax.linalg.ormqr at
+ * lineax/_solver/qr.py:86 (Q, minimum-norm solutions) and :89 (Qᵀ, least
+ * squares). */
+int64_t lxgb_ormqr_workspace_size(int64_t m, int32_t nrhs);
+int lxgb_ormqr_f64(int64_t m, int64_t n, const double* h, const double* tau,
+                   const double* t, int32_t nrhs, double* c, int32_t trans,
+                   void* work, int64_t work_bytes, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Krylov solvers (k right-hand sides at once, FP64).                        */
+/* ------------------------------------------------------------------------ */
+/* lineax runs CG and GMRES as lax.while_loops (cg.py:209, gmres.py:215,292).
+ * Here the host drives the loop and forms operator / preconditioner products
+ * (the operator may be a user function); the entry points below run the rest
+ * of each iteration on the device.  Every right-hand side carries device-side
+ * flags double-buffered by iteration parity: a right-hand side that has
+ * stopped is left untouched by later launches, so the host may run past
+ * convergence and check the flags (…_status) only now and then.  Vectors of
+ * a block are k vectors of length n back to back.  Workspaces need no
+ * initialisation and must be 256-byte aligned. */
+
+/* CG (lineax/_solver/cg.py:114-227).  Host sequence per iteration, parity
+ * p = iteration & 1:  mat_p = A p;  lxgb_cg_step_alpha (alpha with the
+ * breakdown guard, y += alpha p, r -= alpha A p unless cheap_r == 0);  on a
+ * stabilising step  ay = A y, lxgb_cg_true_residual;  z = M r;
+ * lxgb_cg_step_beta (gamma, beta, step, two-space stopping test, p = z + beta
+ * p).  Before the loop: r = b - A y0, z = M r, lxgb_cg_start. */
+int64_t lxgb_cg_workspace_size(int32_t nrhs, int64_t n);
+int lxgb_cg_start(int32_t k, int64_t n, const double* r, const double* z,
+                  double* p, int64_t max_steps, int32_t has_scale, void* work,
+                  int64_t work_bytes, void* stream);
+int lxgb_cg_step_alpha(int32_t k, int64_t n, const double* mat_p, double* p,
+                       double* y, double* r, int32_t cheap_r, int32_t parity,
+                       double rtol, double atol, double rcond, void* work,
+                       int64_t work_bytes, void* stream);
+int lxgb_cg_true_residual(int32_t k, int64_t n, const double* b,
+                          const double* ay, double* r, int32_t parity,
+                          void* work, int64_t work_bytes, void* stream);
+int lxgb_cg_step_beta(int32_t k, int64_t n, const double* b, const double* r,
+                      const double* z, double* p, int32_t parity,
+                      int64_t max_steps, int32_t has_scale, double rtol,
+                      double atol, void* work, int64_t work_bytes,
+                      void* stream);
+/* steps[c], active[c] (device int32) for the flags of the given parity. */
+int lxgb_cg_status(int32_t k, int64_t n, int32_t parity, int32_t* steps,
+                   int32_t* active, void* work, int64_t work_bytes,
+                   void* stream);
+
+/* GMRES (lineax/_solver/gmres.py:106-413), restart <= 128.  Host sequence per
+ * outer iteration (parity p): unless first pass, lxgb_gmres_cycle_begin(r),
+ * then for kk < restart: w = M A V[kk] (V[kk] of right-hand side c at work +
+ * lxgb_gmres_basis_offset(...) + c*(restart+1)*n doubles), lxgb_gmres_arnoldi;
+ * lxgb_gmres_cycle_end (least squares, y += V z, diff); t = M(b - A y);
+ * lxgb_gmres_outer (r = t, stagnation, deferred breakdown, stopping test).
+ * Start with lxgb_gmres_init, r = 0, diff = +inf. */
+int64_t lxgb_gmres_workspace_size(int32_t nrhs, int64_t n, int32_t restart);
+int64_t lxgb_gmres_basis_offset(int32_t k, int64_t n, int32_t restart,
+                                int32_t kk);
+int lxgb_gmres_init(int32_t k, int64_t n, int32_t restart, void* work,
+                    int64_t work_bytes, void* stream);
+int lxgb_gmres_cycle_begin(int32_t k, int64_t n, int32_t restart,
+                           int32_t parity, const double* r, void* work,
+                           int64_t work_bytes, void* stream);
+int lxgb_gmres_arnoldi(int32_t k, int64_t n, int32_t restart, int32_t parity,
+                       int32_t kk, double* w, int32_t* on, void* work,
+                       int64_t work_bytes, void* stream);
+int lxgb_gmres_cycle_end(int32_t k, int64_t n, int32_t restart,
+                         int32_t parity, int32_t first, double* y,
+                         double* diff, void* work, int64_t work_bytes,
+                         void* stream);
+int lxgb_gmres_outer(int32_t k, int64_t n, int32_t restart, int32_t parity,
+                     int32_t first, const double* b, const double* t,
+                     double* r, const double* diff, const double* y,
+                     double rtol, double atol, int64_t max_steps,
+                     int32_t stagnation_iters, int32_t has_scale, void* work,
+                     int64_t work_bytes, void* stream);
+/* Per right-hand side 5 ints: active (next), steps, stagnation counter,
+ * breakdown (deferred), not-converged at the last test. */
+int lxgb_gmres_status(int32_t k, int64_t n, int32_t restart, int32_t parity,
+                      int32_t* out, void* work, int64_t work_bytes,
+                      void* stream);
+
+/* Batched k-vector reductions into out[c] (device): op 0 <x_c, y_c>,
+ * 1 max |x_c| (NaN propagates), 2 sum x_c².  Vector c at x + c*ldx. */
+int64_t lxgb_kreduce_workspace_size(int32_t k, int64_t n);
+int lxgb_kreduce_f64(int32_t op, int32_t k, int64_t n, const double* x,
+                     int64_t ldx, const double* y, int64_t ldy, double* out,
+                     void* work, int64_t work_bytes, void* stream);
+
+/* 5-point negative Laplacian on an nx×ny interior grid with zero Dirichlet
+ * boundary, times `scale`, applied to k grids back to back (the matrix-free
+ * FunctionLinearOperator of the CG benchmark configuration). */
+int lxgb_poisson5_f64(int64_t nx, int64_t ny, int32_t k, double scale,
+                      const double* u, double* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */
 

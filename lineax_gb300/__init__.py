@@ -15,6 +15,7 @@ from ._operator import (
     FunctionLinearOperator,
     IdentityLinearOperator,
     MatrixLinearOperator,
+    Poisson2DOperator,
     has_unit_diagonal,
     is_diagonal,
     is_lower_triangular,

@@ -114,9 +114,48 @@ def cho_solve(u: torch.Tensor, b: torch.Tensor, negate: bool = False) -> torch.T
 def trsv(t: torch.Tensor, b: torch.Tensor, *, lower: bool, trans: bool, unit: bool):
     """Solve op(T) x = b; b is (n,) or (nrhs, n)."""
     t = as_f64(t)
-    n = t.shape[0]
+    n = t.shape[0]  # order of the triangle; rows of t may be longer (ld = t.stride(0))
     x = as_f64(b).clone()
     nrhs = 1 if x.ndim == 1 else x.shape[0]
     _ffi.call("lxgb_trsm_f64", n, nrhs, _ffi.ptr(t), t.stride(0), int(lower), int(trans),
               int(unit), _ffi.ptr(x), _stream(t))
+    return x
+
+
+# -- QR -----------------------------------------------------------------------
+
+
+def _workspace(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def geqrf(a: torch.Tensor, already_transposed: bool = False):
+    """Householder QR of the tall matrix M (a = M, or a = Mᵀ when
+    already_transposed).  Returns (h, tau, t) with h = n×m in jnp.linalg.qr's
+    raw layout and t the per-panel compact-WY T blocks."""
+    a = as_f64(a)
+    if already_transposed:
+        n, m = a.shape
+    else:
+        m, n = a.shape
+    lib = _ffi.load()
+    h = torch.empty((n, m), dtype=torch.float64, device=a.device)
+    tau = torch.empty(n, dtype=torch.float64, device=a.device)
+    t = torch.empty(max(1, int(lib.lxgb_geqrf_t_elems(n))), dtype=torch.float64, device=a.device)
+    wbytes = int(lib.lxgb_geqrf_workspace_size(m, n))
+    work = _workspace(wbytes, a.device)
+    _ffi.call("lxgb_geqrf_f64", m, n, _ffi.ptr(a), int(already_transposed), _ffi.ptr(h),
+              _ffi.ptr(tau), _ffi.ptr(t), _ffi.ptr(work), work.numel(), _stream(a))
+    return h, tau, t
+
+
+def ormqr(h: torch.Tensor, tau: torch.Tensor, t: torch.Tensor, c: torch.Tensor, trans: bool):
+    """Qᵀ c (trans) or Q c for c of shape (m,) or (nrhs, m); returns a new tensor."""
+    n, m = h.shape
+    x = as_f64(c).clone()
+    nrhs = 1 if x.ndim == 1 else x.shape[0]
+    wbytes = int(_ffi.load().lxgb_ormqr_workspace_size(m, nrhs))
+    work = _workspace(wbytes, h.device)
+    _ffi.call("lxgb_ormqr_f64", m, n, _ffi.ptr(h), _ffi.ptr(tau), _ffi.ptr(t), nrhs, _ffi.ptr(x),
+              int(trans), _ffi.ptr(work), work.numel(), _stream(h))
     return x

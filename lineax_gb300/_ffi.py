@@ -44,6 +44,40 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
          c_p],
     ),
+    "lxgb_geqrf_t_elems": (c_i64, [c_i64]),
+    "lxgb_geqrf_workspace_size": (c_i64, [c_i64, c_i64]),
+    "lxgb_geqrf_f64": (ctypes.c_int, [c_i64, c_i64, c_p, c_i32, c_p, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_ormqr_workspace_size": (c_i64, [c_i64, c_i32]),
+    "lxgb_ormqr_f64": (
+        ctypes.c_int, [c_i64, c_i64, c_p, c_p, c_p, c_i32, c_p, c_i32, c_p, c_i64, c_p]),
+    "lxgb_cg_workspace_size": (c_i64, [c_i32, c_i64]),
+    "lxgb_cg_start": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_i64, c_i32, c_p, c_i64, c_p]),
+    "lxgb_cg_step_alpha": (
+        ctypes.c_int,
+        [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i32, c_i32, c_f64, c_f64, c_f64, c_p, c_i64, c_p]),
+    "lxgb_cg_true_residual": (
+        ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_i32, c_p, c_i64, c_p]),
+    "lxgb_cg_step_beta": (
+        ctypes.c_int,
+        [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i32, c_i64, c_i32, c_f64, c_f64, c_p, c_i64, c_p]),
+    "lxgb_cg_status": (ctypes.c_int, [c_i32, c_i64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_workspace_size": (c_i64, [c_i32, c_i64, c_i32]),
+    "lxgb_gmres_basis_offset": (c_i64, [c_i32, c_i64, c_i32, c_i32]),
+    "lxgb_gmres_init": (ctypes.c_int, [c_i32, c_i64, c_i32, c_p, c_i64, c_p]),
+    "lxgb_gmres_cycle_begin": (ctypes.c_int, [c_i32, c_i64, c_i32, c_i32, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_arnoldi": (
+        ctypes.c_int, [c_i32, c_i64, c_i32, c_i32, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_cycle_end": (
+        ctypes.c_int, [c_i32, c_i64, c_i32, c_i32, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_outer": (
+        ctypes.c_int,
+        [c_i32, c_i64, c_i32, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_f64, c_f64, c_i64, c_i32,
+         c_i32, c_p, c_i64, c_p]),
+    "lxgb_gmres_status": (ctypes.c_int, [c_i32, c_i64, c_i32, c_i32, c_p, c_p, c_i64, c_p]),
+    "lxgb_kreduce_workspace_size": (c_i64, [c_i32, c_i64]),
+    "lxgb_kreduce_f64": (
+        ctypes.c_int, [c_i32, c_i32, c_i64, c_p, c_i64, c_p, c_i64, c_p, c_p, c_i64, c_p]),
+    "lxgb_poisson5_f64": (ctypes.c_int, [c_i64, c_i64, c_i32, c_f64, c_p, c_p, c_p]),
     "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
     "lxgb_gemv_f64": (
         ctypes.c_int,

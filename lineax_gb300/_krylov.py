@@ -1,0 +1,218 @@
+"""Host drivers of the device Krylov solvers (CG, GMRES) for a block of k
+right-hand sides.
+
+The loop structure restates lineax/_solver/cg.py:114-227 and
+lineax/_solver/gmres.py:106-413; every vector operation and reduction of the
+loop body runs in liblxgb.so (lxgb_cg_* / lxgb_gmres_*).  Operator and
+preconditioner products are formed here: MatrixLinearOperator through
+lxgb_gemv_f64, operators with a ``mv_block`` method (e.g. the Poisson stencil)
+on a whole (k, n) block, and other FunctionLinearOperators vector by vector.
+Each right-hand side has device-side flags, so the host checks convergence
+only every few iterations; iterations past a right-hand side's stop leave it
+untouched, which makes every right-hand side's result the same as when it is
+solved alone.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+
+import torch
+
+from . import _blas, _ffi
+from ._operator import IdentityLinearOperator, MatrixLinearOperator
+from ._structure import ravel, tree_flatten, unravel
+
+SUCCESSFUL, MAX_STEPS_REACHED, SINGULAR, BREAKDOWN, STAGNATION = 0, 1, 2, 3, 4
+EPS64 = 2.220446049250313e-16
+
+
+def _stream(dev) -> int:
+    return _ffi.stream_handle(dev)
+
+
+def _work(nbytes: int, dev) -> torch.Tensor:
+    """FP64-typed scratch of at least nbytes (torch's caching allocator returns
+    512-byte aligned blocks, as the workspaces require)."""
+    return torch.empty(max(int(nbytes), 256) // 8 + 1, dtype=torch.float64, device=dev)
+
+
+def block_mv(operator, x: torch.Tensor) -> torch.Tensor:
+    """operator applied to each row of the (k, n) float64 block x."""
+    if isinstance(operator, IdentityLinearOperator):
+        return x
+    if isinstance(operator, MatrixLinearOperator):
+        return _blas.gemv(operator.matrix, x)
+    if hasattr(operator, "mv_block"):
+        return operator.mv_block(x)
+    ins = operator.in_structure()
+    rows = [ravel(operator.mv(unravel(x[c], ins)), torch.float64) for c in range(x.shape[0])]
+    return torch.stack(rows).contiguous()
+
+
+def _check_schedule(it: int) -> bool:
+    """Iterations after which the host reads the flags: every iteration for the
+    first 8, then every 8th (stopped right-hand sides are frozen meanwhile)."""
+    return it < 8 or (it + 1) % 8 == 0
+
+
+@dataclasses.dataclass
+class KrylovResult:
+    y: torch.Tensor          # (k, n) solutions
+    steps: list              # per right-hand side
+    results: list            # RESULTS codes per right-hand side
+
+
+def cg_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+             stabilise_every=10, preconditioner=None, y0: torch.Tensor | None = None
+             ) -> KrylovResult:
+    """CG on the (k, n) block b (operator positive definite)."""
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    k, n = b.shape
+    dev = b.device
+    size = n
+    max_steps_ = 10 * size if max_steps is None else int(max_steps)
+    has_scale = not (atol == 0 and rtol == 0)
+    rcond = 2 * EPS64 * size  # lineax/_misc.py:30-38
+    pre = preconditioner if preconditioner is not None else None
+    y = (torch.zeros_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone())
+    wbytes = int(_ffi.load().lxgb_cg_workspace_size(k, n))
+    work = _work(wbytes, dev)
+    st = _stream(dev)
+    r = (b - block_mv(operator, y)).contiguous() if y0 is not None else b.clone()
+    z = block_mv(pre, r).contiguous() if pre is not None else r
+    p = torch.empty_like(b)
+    _ffi.call("lxgb_cg_start", k, n, _ffi.ptr(r), _ffi.ptr(z), _ffi.ptr(p), max_steps_,
+              int(has_scale), _ffi.ptr(work), work.numel() * 8, st)
+    steps_d = torch.empty(k, dtype=torch.int32, device=dev)
+    act_d = torch.empty(k, dtype=torch.int32, device=dev)
+
+    def status(parity):
+        _ffi.call("lxgb_cg_status", k, n, parity, _ffi.ptr(steps_d), _ffi.ptr(act_d),
+                  _ffi.ptr(work), work.numel() * 8, st)
+        return steps_d.cpu().tolist(), act_d.cpu().tolist()
+
+    _, act = status(0)
+    it = 0
+    while any(act) and it < max_steps_:
+        par = it & 1
+        mat_p = block_mv(operator, p)
+        step_no = it + 1
+        if stabilise_every == 1:
+            stable = True
+        elif stabilise_every is None:
+            stable = False
+        else:
+            stable = step_no % stabilise_every == 0
+        _ffi.call("lxgb_cg_step_alpha", k, n, _ffi.ptr(mat_p), _ffi.ptr(p), _ffi.ptr(y),
+                  _ffi.ptr(r), int(not stable), par, float(rtol), float(atol), rcond,
+                  _ffi.ptr(work), work.numel() * 8, st)
+        if stable:
+            ay = block_mv(operator, y)
+            _ffi.call("lxgb_cg_true_residual", k, n, _ffi.ptr(b), _ffi.ptr(ay), _ffi.ptr(r),
+                      par, _ffi.ptr(work), work.numel() * 8, st)
+        z = block_mv(pre, r).contiguous() if pre is not None else r
+        _ffi.call("lxgb_cg_step_beta", k, n, _ffi.ptr(b), _ffi.ptr(r), _ffi.ptr(z), _ffi.ptr(p),
+                  par, max_steps_, int(has_scale), float(rtol), float(atol), _ffi.ptr(work),
+                  work.numel() * 8, st)
+        if _check_schedule(it):
+            _, act = status(par ^ 1)
+        it += 1
+    steps, _ = status(it & 1)
+    results = []
+    for s in steps:
+        if max_steps is None:
+            results.append(SINGULAR if s == max_steps_ else SUCCESSFUL)
+        elif has_scale:
+            results.append(MAX_STEPS_REACHED if s == max_steps_ else SUCCESSFUL)
+        else:
+            results.append(SUCCESSFUL)
+    return KrylovResult(y, steps, results)
+
+
+def gmres_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+                restart=20, stagnation_iters=20, preconditioner=None,
+                y0: torch.Tensor | None = None) -> KrylovResult:
+    """Restarted GMRES on the (k, n) block b."""
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    k, n = b.shape
+    dev = b.device
+    size = n
+    max_steps_ = 10 * size if max_steps is None else int(max_steps)
+    has_scale = not (atol == 0 and rtol == 0)
+    R = min(int(restart), size)
+    if R > 128:
+        raise ValueError("lineax_gb300 GMRES supports restart <= 128")
+    lib = _ffi.load()
+    wbytes = int(lib.lxgb_gmres_workspace_size(k, n, R))
+    work = _work(wbytes, dev)
+    st = _stream(dev)
+    pre = preconditioner
+
+    def mpre(x):
+        return block_mv(pre, x).contiguous() if pre is not None else x
+
+    y = torch.zeros_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone()
+    r = torch.zeros_like(b)
+    diff = torch.full_like(b, float("inf"))
+    on = torch.empty(k, dtype=torch.int32, device=dev)
+    stat = torch.empty((k, 5), dtype=torch.int32, device=dev)
+    _ffi.call("lxgb_gmres_init", k, n, R, _ffi.ptr(work), work.numel() * 8, st)
+    work_f64 = work
+    base_off = [int(lib.lxgb_gmres_basis_offset(k, n, R, kk)) // 8 for kk in range(R + 1)]
+
+    def status(parity):
+        _ffi.call("lxgb_gmres_status", k, n, R, parity, _ffi.ptr(stat), _ffi.ptr(work),
+                  work.numel() * 8, st)
+        return stat.cpu().tolist()
+
+    it = 0
+    while True:
+        par = it & 1
+        first = it == 0
+        if not first:
+            _ffi.call("lxgb_gmres_cycle_begin", k, n, R, par, _ffi.ptr(r), _ffi.ptr(work),
+                      work.numel() * 8, st)
+            for kk in range(R):
+                vk = torch.as_strided(work_f64, (k, n), ((R + 1) * n, 1), base_off[kk])
+                w = mpre(block_mv(operator, vk)).contiguous()
+                if w.data_ptr() == vk.data_ptr():
+                    w = w.clone()
+                _ffi.call("lxgb_gmres_arnoldi", k, n, R, par, kk, _ffi.ptr(w), _ffi.ptr(on),
+                          _ffi.ptr(work), work.numel() * 8, st)
+        _ffi.call("lxgb_gmres_cycle_end", k, n, R, par, int(first), _ffi.ptr(y), _ffi.ptr(diff),
+                  _ffi.ptr(work), work.numel() * 8, st)
+        t = mpre((b - block_mv(operator, y)).contiguous()).contiguous()
+        _ffi.call("lxgb_gmres_outer", k, n, R, par, int(first), _ffi.ptr(b), _ffi.ptr(t),
+                  _ffi.ptr(r), _ffi.ptr(diff), _ffi.ptr(y), float(rtol), float(atol), max_steps_,
+                  int(stagnation_iters), int(has_scale), _ffi.ptr(work), work.numel() * 8, st)
+        it += 1
+        rows = status(it & 1)
+        if not any(row[0] for row in rows) or it >= max_steps_ + 1:
+            break
+    results, steps = [], []
+    for active, s, stag, deferred, nc in rows:
+        if max_steps is None:
+            res = SINGULAR if s == max_steps_ else SUCCESSFUL
+        elif has_scale:
+            res = MAX_STEPS_REACHED if s == max_steps_ else SUCCESSFUL
+        else:
+            res = SUCCESSFUL
+        if stag >= stagnation_iters:
+            res = STAGNATION
+        if deferred and nc:
+            res = BREAKDOWN
+        results.append(res)
+        steps.append(s)
+    return KrylovResult(y, steps, results)
+
+
+def vector_block(vector):
+    """(k=1, n) float64 block of a lineax vector PyTree, and its structure."""
+    leaves, _ = tree_flatten(vector)
+    flat = ravel(vector, torch.float64).contiguous()
+    return flat.reshape(1, -1), leaves

@@ -254,3 +254,41 @@ def materialise(op) -> MatrixLinearOperator:
     eye = torch.eye(n, dtype=dtype, device="cuda")
     cols = [ravel(op.mv(unravel(eye[j], ins)), dtype) for j in range(n)]
     return MatrixLinearOperator(torch.stack(cols, dim=1).contiguous(), op.tags)
+
+
+def conj_not_needed(state, options):
+    """conj of a solver state over real operators is the state itself (complex
+    dtypes are rejected when the operator is built)."""
+    return state, options
+
+
+class Poisson2DOperator(FunctionLinearOperator):
+    """The 5-point negative Laplacian on an nx×ny interior grid with zero
+    Dirichlet boundary (times `scale`), matrix-free on lxgb_poisson5_f64: the
+    FunctionLinearOperator of the CG benchmark configuration.  Positive
+    definite and symmetric.  Vectors are flattened grids (length nx·ny)."""
+
+    def __init__(self, nx: int, ny: int, scale: float = 1.0, dtype=torch.float64):
+        self.nx, self.ny, self.scale = int(nx), int(ny), float(scale)
+        super().__init__(self._apply, ShapeDtypeStruct((self.nx * self.ny,), dtype),
+                         (symmetric_tag, positive_semidefinite_tag))
+
+    def _apply(self, x):
+        return self.mv_block(x.reshape(1, -1)).reshape(x.shape)
+
+    def mv_block(self, x):
+        from . import _ffi
+        from ._blas import as_device_f64
+
+        xb = as_device_f64(x)
+        k = xb.shape[0]
+        out = torch.empty_like(xb)
+        _ffi.call("lxgb_poisson5_f64", self.nx, self.ny, k, self.scale, _ffi.ptr(xb),
+                  _ffi.ptr(out), _ffi.stream_handle(xb.device))
+        return out
+
+    def transpose(self):
+        return self
+
+    def as_matrix(self):
+        return materialise(self).matrix

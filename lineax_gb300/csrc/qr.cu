@@ -1,0 +1,478 @@
+// Householder QR (geqrf) and application of Q / Qᵀ (ormqr), FP64.
+//
+// Storage: the factor is kept in the "raw" layout JAX's jnp.linalg.qr(mode=
+// "raw") returns, h = Mᵀ (nn rows of length mm) for a tall mm×nn matrix M, so
+// every column of M — every Householder vector — is a contiguous row of h.
+// On return h[k][k..] holds R's k-th column on and above the diagonal (R[i][k] =
+// h[k][i], i <= k) and the k-th reflector below it (v_k[i] = h[k][i], i > k,
+// v_k[k] = 1), tau[k] its scalar: H_k = I - tau_k v_k v_kᵀ, Q = H_0 H_1 ...
+//
+// Blocked right-looking with compact-WY panels of kQrNB reflectors
+// (H_j0 ... H_{j0+nb-1} = I - V T Vᵀ, T upper triangular):
+//   qr_panel_kernel   — the reflectors of one panel (LAPACK geqr2/larfg rules)
+//   qr_larft_kernel   — T of the panel (larft, forward column-wise)
+//   qr_w_kernel       — W = Vᵀ C for the trailing columns C (split over rows)
+//   qr_wt_kernel      — W' = Tᵀ W (summing the splits in fixed order)
+//   qr_update_kernel  — C -= V W'  (64×64 tiles, K = nb)
+// T of every panel is kept so that ormqr applies whole panels at once.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace lxgb {
+
+constexpr int kQrNB = 32;
+constexpr int kQrPanelThreads = 512;
+
+// v_p[i] for panel row p (global row r = j0 + p) read from h.
+__device__ __forceinline__ double refl(const double* h, int64_t mm, int r, int64_t i) {
+  return (i < r) ? 0.0 : (i == r ? 1.0 : h[(int64_t)r * mm + i]);
+}
+
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < nw; ++w) t += red[w];
+  return t;
+}
+
+// Reflectors of panel rows [j0, pe) of h (mm columns).
+__global__ void __launch_bounds__(kQrPanelThreads)
+qr_panel_kernel(int64_t mm, int nn, int j0, int pe, double* __restrict__ h,
+                double* __restrict__ tau) {
+  __shared__ double red[32];
+  __shared__ double wred[kQrPanelThreads / 32][kQrNB];
+  __shared__ double s_tau, s_scal;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = blockDim.x >> 5;
+  for (int k = j0; k < pe; ++k) {
+    double* hk = h + (int64_t)k * mm;
+    double ss = 0.0;
+    for (int64_t i = k + 1 + tid; i < mm; i += blockDim.x) ss = fma(hk[i], hk[i], ss);
+    const double xnorm2 = block_sum(ss, red);
+    if (tid == 0) {
+      const double alpha = hk[k];
+      const double xnorm = sqrt(xnorm2);
+      if (xnorm == 0.0) {
+        s_tau = 0.0;
+        s_scal = 1.0;
+      } else {
+        const double beta = -copysign(hypot(alpha, xnorm), alpha);
+        s_tau = (beta - alpha) / beta;
+        s_scal = 1.0 / (alpha - beta);
+        hk[k] = beta;
+      }
+      tau[k] = s_tau;
+    }
+    __syncthreads();
+    const double tk = s_tau;
+    if (tk != 0.0) {
+      const double sc = s_scal;
+      for (int64_t i = k + 1 + tid; i < mm; i += blockDim.x) hk[i] *= sc;
+    }
+    __syncthreads();
+    const int nrem = pe - k - 1;
+    if (tk != 0.0 && nrem > 0) {
+      double acc[kQrNB];
+#pragma unroll
+      for (int q = 0; q < kQrNB; ++q) acc[q] = 0.0;
+      for (int64_t i = k + 1 + tid; i < mm; i += blockDim.x) {
+        const double vi = hk[i];
+#pragma unroll
+        for (int q = 0; q < kQrNB; ++q)
+          if (q < nrem) acc[q] = fma(vi, h[(int64_t)(k + 1 + q) * mm + i], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < kQrNB; ++q) {
+        if (q < nrem) {
+          const double s = warp_sum(acc[q]);
+          if (lane == 0) wred[warp][q] = s;
+        }
+      }
+      __syncthreads();
+      // w_j = h[j][k] + sum_{i>k} v_i h[j][i]; then h[j][i] -= tau w_j v_i, i >= k.
+      for (int q = warp; q < nrem; q += nw) {
+        double w = 0.0;
+        for (int ww = 0; ww < nw; ++ww) w += wred[ww][q];
+        double* hj = h + (int64_t)(k + 1 + q) * mm;
+        w += hj[k];
+        const double tw = tk * w;
+        if (lane == 0) hj[k] -= tw;
+        for (int64_t i = k + 1 + lane; i < mm; i += 32) hj[i] = fma(-tw, hk[i], hj[i]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// T (nb×nb, upper) of panel rows [j0, j0+nb): T[k][k] = tau_k and
+// T[0:k, k] = -tau_k T[0:k, 0:k] (V[:, 0:k]ᵀ v_k).
+__global__ void __launch_bounds__(512)
+qr_larft_kernel(int64_t mm, int j0, int nb, const double* __restrict__ h,
+                const double* __restrict__ tau, double* __restrict__ t_out) {
+  __shared__ double G[kQrNB][kQrNB + 1];
+  __shared__ double T[kQrNB][kQrNB + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // G[q][k] = v_qᵀ v_k for q < k (rows i >= j0 + k contribute).
+  for (int pair = warp; pair < nb * nb; pair += nw) {
+    const int q = pair / nb, k = pair % nb;
+    if (q >= k) continue;
+    const int rk = j0 + k, rq = j0 + q;
+    double acc = 0.0;
+    for (int64_t i = rk + lane; i < mm; i += 32)
+      acc = fma(refl(h, mm, rq, i), refl(h, mm, rk, i), acc);
+    acc = warp_sum(acc);
+    if (lane == 0) G[q][k] = acc;
+  }
+  for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x) T[e / kQrNB][e % kQrNB] = 0.0;
+  __syncthreads();
+  if (warp == 0) {
+    for (int k = 0; k < nb; ++k) {
+      const double tk = tau[j0 + k];
+      // lane i < k: T[i][k] = -tk * sum_{q=i}^{k-1} T[i][q] G[q][k]
+      double v = 0.0;
+      if (lane < k) {
+        for (int q = lane; q < k; ++q) v = fma(T[lane][q], G[q][k], v);
+        v = -tk * v;
+      }
+      __syncwarp();
+      if (lane < k) T[lane][k] = v;
+      if (lane == k) T[k][k] = tk;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
+    t_out[e] = T[e / kQrNB][e % kQrNB];
+}
+
+// W_part[s][p][j] = sum_{i in split s} v_p[i] h[j][i] for trailing rows j.
+constexpr int kWRows = 32, kWChunk = 64;
+__global__ void __launch_bounds__(256)
+qr_w_kernel(int64_t mm, int nn, int j0, int nb, const double* __restrict__ h,
+            double* __restrict__ wpart, int64_t split_len) {
+  __shared__ double Vs[kQrNB][kWChunk + 1];
+  __shared__ double Hs[kWRows][kWChunk + 1];
+  const int s = blockIdx.y;
+  const int jbase = j0 + nb + blockIdx.x * kWRows;
+  const int n2 = nn - (j0 + nb);
+  const int64_t i_lo = j0 + (int64_t)s * split_len;
+  const int64_t i_hi = min((int64_t)mm, i_lo + split_len);
+  const int p = threadIdx.x & 31;        // reflector
+  const int jg = threadIdx.x >> 5;       // 8 groups of 4 rows
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t c0 = i_lo; c0 < i_hi; c0 += kWChunk) {
+    for (int e = threadIdx.x; e < kQrNB * kWChunk; e += blockDim.x) {
+      const int pp = e / kWChunk, cc = e % kWChunk;
+      const int64_t i = c0 + cc;
+      Vs[pp][cc] = (pp < nb && i < i_hi) ? refl(h, mm, j0 + pp, i) : 0.0;
+    }
+    for (int e = threadIdx.x; e < kWRows * kWChunk; e += blockDim.x) {
+      const int jj = e / kWChunk, cc = e % kWChunk;
+      const int64_t i = c0 + cc;
+      const int j = jbase + jj;
+      Hs[jj][cc] = (j < nn && i < i_hi) ? h[(int64_t)j * mm + i] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int cc = 0; cc < kWChunk; ++cc) {
+      const double v = Vs[p][cc];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[r] = fma(v, Hs[jg * 4 + r][cc], acc[r]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int jj = blockIdx.x * kWRows + jg * 4 + r;
+    if (p < nb && jj < n2) wpart[((int64_t)s * kQrNB + p) * n2 + jj] = acc[r];
+  }
+}
+
+// W2[p][j] = sum_q T[q][p] * (sum_s W_part[s][q][j])   (Tᵀ W)
+__global__ void qr_wt_kernel(int n2, int nb, int splits, const double* __restrict__ wpart,
+                             const double* __restrict__ T, double* __restrict__ w2) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n2) return;
+  double w[kQrNB];
+#pragma unroll
+  for (int q = 0; q < kQrNB; ++q) {
+    double acc = 0.0;
+    if (q < nb)
+      for (int s = 0; s < splits; ++s) acc += wpart[((int64_t)s * kQrNB + q) * n2 + j];
+    w[q] = acc;
+  }
+#pragma unroll
+  for (int p = 0; p < kQrNB; ++p) {
+    if (p >= nb) break;
+    double acc = 0.0;
+    for (int q = 0; q <= p; ++q) acc = fma(T[q * kQrNB + p], w[q], acc);
+    w2[(int64_t)p * n2 + j] = acc;
+  }
+}
+
+// h[j][i] -= sum_p W2[p][j] v_p[i] for trailing rows j, columns i >= j0.
+constexpr int kUT = 64;
+__global__ void __launch_bounds__(256)
+qr_update_kernel(int64_t mm, int nn, int j0, int nb, double* __restrict__ h,
+                 const double* __restrict__ w2) {
+  __shared__ double Ws[kQrNB][kUT + 1];
+  __shared__ double Vs[kQrNB][kUT + 1];
+  const int n2 = nn - (j0 + nb);
+  const int jt = blockIdx.y * kUT;            // trailing row tile
+  const int64_t it = j0 + (int64_t)blockIdx.x * kUT;
+  for (int e = threadIdx.x; e < kQrNB * kUT; e += blockDim.x) {
+    const int p = e / kUT, c = e % kUT;
+    const int jj = jt + c;
+    Ws[p][c] = (p < nb && jj < n2) ? w2[(int64_t)p * n2 + jj] : 0.0;
+    const int64_t i = it + c;
+    Vs[p][c] = (p < nb && i < mm) ? refl(h, mm, j0 + p, i) : 0.0;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int jj = jt + ty + 16 * r;
+      const int64_t i = it + tx + 16 * c;
+      acc[r][c] = (jj < n2 && i < mm) ? h[(int64_t)(j0 + nb + jj) * mm + i] : 0.0;
+    }
+  for (int p = 0; p < nb; ++p) {
+    double wv[4], vv[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) wv[r] = Ws[p][ty + 16 * r];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) vv[c] = Vs[p][tx + 16 * c];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] = fma(-wv[r], vv[c], acc[r][c]);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int jj = jt + ty + 16 * r;
+      const int64_t i = it + tx + 16 * c;
+      if (jj < n2 && i < mm) h[(int64_t)(j0 + nb + jj) * mm + i] = acc[r][c];
+    }
+}
+
+// h = Mᵀ from M (mm×nn row-major) through 32×32 shared-memory tiles.
+__global__ void transpose_kernel(int64_t rows, int64_t cols, const double* __restrict__ src,
+                                 double* __restrict__ dst) {
+  __shared__ double tile[32][33];
+  const int64_t c0 = blockIdx.x * 32LL, r0 = blockIdx.y * 32LL;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[k][threadIdx.x] = src[r * cols + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t c = c0 + k, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[c * rows + r] = tile[threadIdx.x][k];
+  }
+}
+
+__global__ void copy_kernel(int64_t n, const double* __restrict__ src, double* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// ormqr: partial dots part[r][chunk][p] = sum_{i in chunk} v_p[i] c_r[i].
+constexpr int kOrmChunk = 2048;
+__global__ void __launch_bounds__(256)
+ormqr_dots_kernel(int64_t mm, int j0, int nb, const double* __restrict__ h,
+                  const double* __restrict__ c, int nchunks, double* __restrict__ part) {
+  __shared__ double red[8][kQrNB];
+  const int r = blockIdx.y, ch = blockIdx.x;
+  const double* cr = c + (int64_t)r * mm;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t lo = j0 + (int64_t)ch * kOrmChunk;
+  const int64_t hi = min(mm, lo + kOrmChunk);
+  double acc[kQrNB];
+#pragma unroll
+  for (int p = 0; p < kQrNB; ++p) acc[p] = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const double ci = cr[i];
+#pragma unroll
+    for (int p = 0; p < kQrNB; ++p)
+      if (p < nb) acc[p] = fma(refl(h, mm, j0 + p, i), ci, acc[p]);
+  }
+#pragma unroll
+  for (int p = 0; p < kQrNB; ++p) {
+    const double s = warp_sum(acc[p]);
+    if (lane == 0) red[warp][p] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < kQrNB) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += red[w][threadIdx.x];
+    part[((int64_t)r * nchunks + ch) * kQrNB + threadIdx.x] = s;
+  }
+}
+
+// c_r[i] -= sum_p v_p[i] w'[p], w' = op(T) (sum over chunks of part).
+__global__ void __launch_bounds__(256)
+ormqr_apply_kernel(int64_t mm, int j0, int nb, const double* __restrict__ h,
+                   const double* __restrict__ T, int trans, double* __restrict__ c, int nchunks,
+                   const double* __restrict__ part) {
+  __shared__ double w[kQrNB], w2[kQrNB];
+  const int r = blockIdx.y, ch = blockIdx.x;
+  double* cr = c + (int64_t)r * mm;
+  if (threadIdx.x < kQrNB) {
+    double s = 0.0;
+    for (int k = 0; k < nchunks; ++k) s += part[((int64_t)r * nchunks + k) * kQrNB + threadIdx.x];
+    w[threadIdx.x] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < kQrNB) {
+    const int p = threadIdx.x;
+    double s = 0.0;
+    if (p < nb) {
+      if (trans) {  // Qᵀ c: w' = Tᵀ w
+        for (int q = 0; q <= p; ++q) s = fma(T[q * kQrNB + p], w[q], s);
+      } else {      // Q c: w' = T w
+        for (int q = p; q < nb; ++q) s = fma(T[p * kQrNB + q], w[q], s);
+      }
+    }
+    w2[p] = s;
+  }
+  __syncthreads();
+  const int64_t lo = j0 + (int64_t)ch * kOrmChunk;
+  const int64_t hi = min(mm, lo + kOrmChunk);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    double acc = cr[i];
+    for (int p = 0; p < nb; ++p) acc = fma(-refl(h, mm, j0 + p, i), w2[p], acc);
+    cr[i] = acc;
+  }
+}
+
+static int64_t qr_splits(int64_t mm, int n2) {
+  const int64_t jt = (n2 + kWRows - 1) / kWRows;
+  int64_t s = (2LL * sm_count() + jt - 1) / (jt > 0 ? jt : 1);
+  const int64_t cap = (mm + 255) / 256;
+  if (s > cap) s = cap;
+  if (s < 1) s = 1;
+  return s;
+}
+
+}  // namespace lxgb
+
+using namespace lxgb;
+
+extern "C" int64_t lxgb_geqrf_t_elems(int64_t n) {
+  return ((n + kQrNB - 1) / kQrNB) * (int64_t)kQrNB * kQrNB;
+}
+
+// Split geometry of the W = Vᵀ C pass of panel j0 (shared by the size query
+// and the launch so both agree exactly).
+static void qr_w_geometry(int64_t m, int nn, int j0, int nb, int64_t* split_len, int64_t* used) {
+  const int n2 = nn - (j0 + nb);
+  const int64_t span = m - j0;
+  const int64_t splits = qr_splits(span, n2);
+  *split_len = ((span + splits - 1) / splits + kWChunk - 1) / kWChunk * kWChunk;
+  *used = (span + *split_len - 1) / *split_len;
+}
+
+extern "C" int64_t lxgb_geqrf_workspace_size(int64_t m, int64_t n) {
+  if (m <= 0 || n <= 0 || n > m) return 256;
+  int64_t worst = 0;
+  for (int j0 = 0; j0 < n; j0 += kQrNB) {
+    const int nb = (int)(n - j0 < kQrNB ? n - j0 : kQrNB);
+    const int n2 = (int)n - (j0 + nb);
+    if (n2 <= 0) continue;
+    int64_t split_len, used;
+    qr_w_geometry(m, (int)n, j0, nb, &split_len, &used);
+    const int64_t need = (used + 1) * kQrNB * (int64_t)n2;
+    if (need > worst) worst = need;
+  }
+  return 256 + worst * (int64_t)sizeof(double);
+}
+
+extern "C" int lxgb_geqrf_f64(int64_t m, int64_t n, const double* a, int32_t a_layout, double* h,
+                              double* tau, double* t, void* work, int64_t work_bytes,
+                              void* stream) {
+  LXGB_REQUIRE(m >= 0 && n >= 0, "geqrf: negative size");
+  LXGB_REQUIRE(n <= m, "geqrf: needs a tall matrix (n <= m); transpose wide ones");
+  LXGB_REQUIRE(a_layout == 0 || a_layout == 1, "geqrf: a_layout must be 0 or 1");
+  LXGB_REQUIRE(n < (1LL << 31), "geqrf: n too large");
+  if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(a && h && tau && t && work, "geqrf: null pointer");
+  if (work_bytes < lxgb_geqrf_workspace_size(m, n)) {
+    set_last_error("geqrf: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  if (a_layout == 0) {
+    dim3 grid((unsigned)((n + 31) / 32), (unsigned)((m + 31) / 32));
+    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(m, n, a, h);
+  } else if (a != h) {
+    const int64_t cnt = m * n;
+    const int64_t blocks = (cnt + 255) / 256 < 4096 ? (cnt + 255) / 256 : 4096;
+    copy_kernel<<<(unsigned)blocks, 256, 0, st>>>(cnt, a, h);
+  }
+  const int nn = (int)n;
+  double* wbase = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + 256);
+  for (int j0 = 0; j0 < nn; j0 += kQrNB) {
+    const int nb = min(kQrNB, nn - j0);
+    qr_panel_kernel<<<1, kQrPanelThreads, 0, st>>>(m, nn, j0, j0 + nb, h, tau);
+    double* Tp = t + (int64_t)(j0 / kQrNB) * kQrNB * kQrNB;
+    qr_larft_kernel<<<1, 512, 0, st>>>(m, j0, nb, h, tau, Tp);
+    const int n2 = nn - (j0 + nb);
+    if (n2 > 0) {
+      int64_t split_len, used;
+      qr_w_geometry(m, nn, j0, nb, &split_len, &used);
+      double* wpart = wbase;
+      double* w2 = wbase + used * kQrNB * (int64_t)n2;
+      dim3 gw((unsigned)((n2 + kWRows - 1) / kWRows), (unsigned)used);
+      qr_w_kernel<<<gw, 256, 0, st>>>(m, nn, j0, nb, h, wpart, split_len);
+      qr_wt_kernel<<<(n2 + 127) / 128, 128, 0, st>>>(n2, nb, (int)used, wpart, Tp, w2);
+      dim3 gu((unsigned)((m - j0 + kUT - 1) / kUT), (unsigned)((n2 + kUT - 1) / kUT));
+      qr_update_kernel<<<gu, 256, 0, st>>>(m, nn, j0, nb, h, w2);
+    }
+  }
+  return check_launch("geqrf");
+}
+
+extern "C" int64_t lxgb_ormqr_workspace_size(int64_t m, int32_t nrhs) {
+  const int64_t chunks = (m + kOrmChunk - 1) / kOrmChunk;
+  return 256 + (int64_t)(nrhs > 0 ? nrhs : 0) * chunks * kQrNB * (int64_t)sizeof(double);
+}
+
+extern "C" int lxgb_ormqr_f64(int64_t m, int64_t n, const double* h, const double* tau,
+                              const double* t, int32_t nrhs, double* c, int32_t trans, void* work,
+                              int64_t work_bytes, void* stream) {
+  (void)tau;  // the panel T matrices carry the tau values
+  LXGB_REQUIRE(m >= 0 && n >= 0 && n <= m && nrhs >= 0, "ormqr: bad sizes");
+  LXGB_REQUIRE(trans == 0 || trans == 1, "ormqr: trans must be 0 or 1");
+  if (m == 0 || n == 0 || nrhs == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(h && t && c && work, "ormqr: null pointer");
+  LXGB_REQUIRE(nrhs <= 65535, "ormqr: too many vectors");
+  if (work_bytes < lxgb_ormqr_workspace_size(m, nrhs)) {
+    set_last_error("ormqr: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  double* part = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + 256);
+  const int npan = (int)((n + kQrNB - 1) / kQrNB);
+  for (int q = 0; q < npan; ++q) {
+    const int pidx = trans ? q : npan - 1 - q;  // Qᵀ: H_0 first; Q: last panel first
+    const int j0 = pidx * kQrNB;
+    const int nb = (int)(n - j0 < kQrNB ? n - j0 : kQrNB);
+    const int64_t span = m - j0;
+    const int nchunks = (int)((span + kOrmChunk - 1) / kOrmChunk);
+    dim3 g((unsigned)nchunks, (unsigned)nrhs);
+    const double* Tp = t + (int64_t)pidx * kQrNB * kQrNB;
+    ormqr_dots_kernel<<<g, 256, 0, st>>>(m, j0, nb, h, c, nchunks, part);
+    ormqr_apply_kernel<<<g, 256, 0, st>>>(m, j0, nb, h, Tp, trans, c, nchunks, part);
+  }
+  return check_launch("ormqr");
+}
