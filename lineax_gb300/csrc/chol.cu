@@ -19,10 +19,7 @@ constexpr int kCholThreads = 256;
 // Largest order factored in shared memory: FP64 160*161*8 B = 206 KB,
 // FP32 224*225*4 B = 202 KB (+ the correction vectors of the mixed path).
 constexpr int kCholSmemMaxF64 = 160;
-constexpr int kCholSmemMaxF32 = 224;
-constexpr int kMixedRhsChunk = 16;
 constexpr int kQueueHeader = 256;  // bytes reserved for the work-queue counter
-constexpr int kMixedMaxN = 2048;   // one CTA per system; correction vectors in shared memory
 
 // Right-looking blocked upper Cholesky by the whole CTA.  a has row stride ld;
 // only j >= i is read or written.  Each element receives its updates as an FMA
@@ -176,92 +173,660 @@ potrs_ragged_f64_kernel(int64_t batch, int max_n, const int32_t* __restrict__ nv
 }
 
 // ---------------------------------------------------------------------------
-// Mixed precision: FP32 factor, FP64 refinement.
+// Mixed precision: FP32 factor, FP64-accurate refinement.
+//
+// One persistent launch, two 256-thread CTAs per SM, systems from an atomic
+// queue.  Per system:
+//  * factor in FP32 — n <= kMxSmallN: right-looking in shared memory with
+//    16-column panels (diagonal block by one warp, column-parallel TRSM of the
+//    block row, register-tiled SYRK of the trailing matrix: three barriers per
+//    panel); larger n: left-looking by 32-row block rows of U kept in this
+//    CTA's workspace slice (an FP32 n×n array, L2-resident while the CTA works
+//    on it), each block row formed by a register-tiled GEMM that streams the
+//    finished rows of U, then its diagonal block and TRSM;
+//  * all right-hand sides of a chunk (<= 8) solved together with the FP32
+//    factor (blocked forward/backward substitution, one warp per vector on the
+//    32×32 diagonal blocks, all threads on the off-diagonal updates);
+//  * refinement: r = b - A x to FP64 accuracy from the FP64 matrix with
+//    error-free FP32 transformations — A and x are split bitwise into hi+lo
+//    FP32 pairs (|a - hi - lo| <= 2^-46 |a|), hi*hi products are made exact
+//    with an FMA (TwoProd) and summed with TwoSum, lower-order terms in a
+//    second FP32 accumulator.  GB300 issues one FP64 FMA per ~68 FP32 lane
+//    operations, so this costs ~6x less than native FP64 while keeping the
+//    residual's error near 1e-14 of ||A|| ||x||;
+//  * x accumulated in FP64; a right-hand side is frozen once its normwise
+//    backward error is <= tol (its result is the same alone or in a batch).
 // ---------------------------------------------------------------------------
-struct MixedSmem {
-  TrsvSmem<float> tsm;
-  double red[32][kMixedRhsChunk];  // per-warp partial maxima
-  double anorm;
-  double bnorm[kMixedRhsChunk];
-  double berr[kMixedRhsChunk];
-  int done[kMixedRhsChunk];
+constexpr int kMxThreads = 256;
+constexpr int kMxSmallN = 144;   // 144*145*4 B = 82 KB factor in shared memory
+constexpr int kMxKc = 8;         // right-hand sides per refinement chunk
+constexpr int kMxNB = 32;        // block rows of the large path and of the solves
+constexpr int kMxMaxN = 1024;
+
+struct MxSmem {
+  float rd[kMxMaxN];                     // 1 / diagonal of the FP32 factor
+  float red[kMxThreads / 32][kMxKc];     // per-warp partial maxima
+  float red2[kMxThreads / 32][kMxKc + 1];  // [0]: row-sum max, [1 + c]: max |x_c|
+  float anorm;
+  float bnorm[kMxKc];
+  double berr[kMxKc];
+  int done[kMxKc];
   int next;
-  int all_done;
+  int flag;
 };
 
-// r = b - A x for the vectors [r0, r0+nc) of one system, A FP64 read from
-// global memory (one warp per row, lanes along the row).  Writes the FP32
-// copy of r into d, and per-vector max|r| and max|x| into red (per warp).
-__device__ void residual_f64(const double* __restrict__ A, int n, const double* __restrict__ B,
-                             const double* __restrict__ X, int nc, float* d, int ldd,
-                             MixedSmem& sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double rmax[kMixedRhsChunk], xmax[kMixedRhsChunk];
-#pragma unroll
-  for (int c = 0; c < kMixedRhsChunk; ++c) { rmax[c] = 0.0; xmax[c] = 0.0; }
-  for (int i = warp; i < n; i += nw) {
-    double acc[kMixedRhsChunk];
-#pragma unroll
-    for (int c = 0; c < kMixedRhsChunk; ++c) acc[c] = 0.0;
-    const double* row = A + (int64_t)i * n;
-    for (int j = lane; j < n; j += 32) {
-      const double aij = row[j];
-#pragma unroll
-      for (int c = 0; c < kMixedRhsChunk; ++c)
-        if (c < nc) acc[c] = fma(aij, X[(int64_t)c * n + j], acc[c]);
+// hi = a truncated to 24 significant bits, lo = the rest truncated to 24
+// bits, by integer operations only; |a - hi - lo| <= 2^-46 |a|.  Nonzero
+// values outside 2^-74 <= |a| < 2^128 (and inf, NaN) take a conversion path
+// behind a warp-uniform branch: GB300 runs conversions on its narrow FP64
+// pipe, and a predicated (if-converted) fallback would issue them for every
+// element.
+__device__ __forceinline__ void split_f64(double a, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(a);
+  const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const unsigned mh = (unsigned)(u >> 29) & 0x7FFFFFu;
+  const unsigned rem = (unsigned)u & 0x1FFFFFFFu;
+  const int sh = __clz(rem | 1u) - 8;
+  const unsigned m = (sh >= 0) ? (rem << sh) : (rem >> (-sh));
+  const int ex = (int)e - 1052 - sh + 127;
+  const bool zero = (u << 1) == 0ull;
+  hi = zero ? __uint_as_float(sign) : __uint_as_float(sign | (((e - 1023u + 127u) & 0xFFu) << 23) | mh);
+  lo = (rem == 0u) ? 0.0f : __uint_as_float(sign | (((unsigned)ex & 0xFFu) << 23) | (m & 0x7FFFFFu));
+  const bool slow = !zero && ((e < 949u) || (e > 1150u));
+  if (__any_sync(__activemask(), slow)) {
+    if (slow) {
+      hi = __double2float_rz(a);
+      lo = __double2float_rn(a - (double)hi);
     }
+  }
+}
+
+// FP32 copy of a for the factor (the hi part of split_f64, integer path).
+__device__ __forceinline__ float to_f32(double a) {
+  float hi, lo;
+  split_f64(a, hi, lo);
+  return hi;
+}
+
+// s + t exactly as (s', err) (Knuth TwoSum).
+__device__ __forceinline__ void two_sum(float& s, float t, float& err) {
+  const float r = s + t;
+  const float z = r - s;
+  err = (s - (r - z)) + (t - z);
+  s = r;
+}
+
+// Factor the nb×nb diagonal block at F[j0.., j0..] (upper triangle, row
+// stride ld) by one warp entirely in registers: lane j holds column j; row k
+// of U is formed in place and rows i > k updated with u_ki fetched by shuffle.
+// Writes U_JJ back and 1/diag into rd[0..nb).  Returns 0 or (j0+k+1) for the
+// first pivot that is not positive.
+template <int NBMAX>
+__device__ int warp_potrf_block(float* F, int64_t ld, int j0, int nb, float* rd) {
+  const int lane = threadIdx.x & 31;
+  float col[NBMAX];
 #pragma unroll
-    for (int c = 0; c < kMixedRhsChunk; ++c) {
-      if (c < nc) {
-        const double ax = warp_sum(acc[c]);
-        const double r = B[(int64_t)c * n + i] - ax;
-        if (lane == 0) {
-          d[c * ldd + i] = (float)r;
-          rmax[c] = fmax(rmax[c], fabs(r));
-          xmax[c] = fmax(xmax[c], fabs(X[(int64_t)c * n + i]));
+  for (int i = 0; i < NBMAX; ++i)
+    col[i] = (i < nb && i <= lane && lane < nb) ? F[(int64_t)(j0 + i) * ld + j0 + lane] : 0.0f;
+  int bad = 0;
+#pragma unroll
+  for (int k = 0; k < NBMAX; ++k) {
+    if (k < nb && bad == 0) {
+      const float akk = __shfl_sync(0xffffffffu, col[k], k);
+      if (!(akk > 0.0f)) {
+        bad = j0 + k + 1;
+      } else {
+        const float d = sqrtf(akk);
+        const float r = 1.0f / d;
+        if (lane == k) col[k] = d;
+        else if (lane > k) col[k] *= r;
+        if (lane == 0) rd[k] = r;
+#pragma unroll
+        for (int i = k + 1; i < NBMAX; ++i) {
+          if (i < nb) {
+            const float uki = __shfl_sync(0xffffffffu, col[k], i);
+            if (lane >= i) col[i] = fmaf(-uki, col[k], col[i]);
+          }
         }
       }
     }
   }
-  if (lane == 0) {
+  if (bad == 0) {
 #pragma unroll
-    for (int c = 0; c < kMixedRhsChunk; ++c) sm.red[warp][c] = rmax[c];
+    for (int i = 0; i < NBMAX; ++i)
+      if (i < nb && i <= lane && lane < nb) F[(int64_t)(j0 + i) * ld + j0 + lane] = col[i];
   }
-  __syncthreads();
-  // fold per-warp maxima: thread c < nc owns vector c.
-  if (threadIdx.x < nc) {
-    double rm = 0.0;
-    for (int w = 0; w < nw; ++w) rm = fmax(rm, sm.red[w][threadIdx.x]);
-    sm.berr[threadIdx.x] = rm;  // numerator for now
-  }
-  __syncthreads();
-  if (lane == 0) {
+  return bad;
+}
+
+// Rows [kb, kb+nb) of the block row: U[kb:kb+nb, j] = U_kk^{-T} A[kb:kb+nb, j]
+// for columns j in [j_lo, n), one column per thread.
+template <int NBMAX>
+__device__ void block_row_trsm(float* F, int64_t ld, int kb, int nb, int j_lo, int n,
+                               const float* rd) {
+  for (int j = j_lo + threadIdx.x; j < n; j += blockDim.x) {
+    float y[NBMAX];
 #pragma unroll
-    for (int c = 0; c < kMixedRhsChunk; ++c) sm.red[warp][c] = xmax[c];
+    for (int p = 0; p < NBMAX; ++p) y[p] = (p < nb) ? F[(int64_t)(kb + p) * ld + j] : 0.0f;
+#pragma unroll
+    for (int p = 0; p < NBMAX; ++p) {
+      if (p < nb) {
+        float v = y[p];
+#pragma unroll
+        for (int q = 0; q < p; ++q) v = fmaf(-F[(int64_t)(kb + q) * ld + kb + p], y[q], v);
+        y[p] = v * rd[kb + p];
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NBMAX; ++p)
+      if (p < nb) F[(int64_t)(kb + p) * ld + j] = y[p];
+  }
+}
+
+// --- small path: right-looking in shared memory ---------------------------
+// Returns 0 or k+1.  F row stride ld, upper triangle.
+__device__ int mx_factor_small(float* F, int ld, int n, MxSmem& sm) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tx = tid & 15, ty = tid >> 4;
+  for (int kb = 0; kb < n; kb += 16) {
+    const int ke = min(kb + 16, n);
+    if (warp == 0) {
+      const int bad = warp_potrf_block<16>(F, ld, kb, ke - kb, sm.rd + kb);
+      if ((tid & 31) == 0) sm.flag = bad;
+    }
+    __syncthreads();
+    if (sm.flag) return sm.flag;
+    block_row_trsm<16>(F, ld, kb, ke - kb, ke, n, sm.rd);
+    __syncthreads();
+    // trailing update of [ke, n): F[i][j] -= sum_p F[p][i] F[p][j], j >= i
+    const int m = n - ke;
+    if (m > 0) {
+      const int tiles = (m + 63) >> 6;
+      for (int t = 0; t < tiles * tiles; ++t) {
+        const int ti = t / tiles, tj = t % tiles;
+        if (tj < ti) continue;
+        const int i0 = ke + (ti << 6), j0 = ke + (tj << 6);
+        float acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
+            acc[r][c] = (i < n && j < n && j >= i) ? F[i * ld + j] : 0.0f;
+          }
+        for (int p = kb; p < ke; ++p) {
+          float ui[4], uj[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int i = i0 + ty + 16 * r;
+            ui[r] = (i < n) ? F[p * ld + i] : 0.0f;
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int j = j0 + tx + 16 * c;
+            uj[c] = (j < n) ? F[p * ld + j] : 0.0f;
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(-ui[r], uj[c], acc[r][c]);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
+            if (i < n && j < n && j >= i) F[i * ld + j] = acc[r][c];
+          }
+      }
+      __syncthreads();
+    }
+  }
+  return 0;
+}
+
+// --- large path: left-looking by 32-row block rows, U in global -----------
+// U has row stride ldu (n rounded up to 32) so that every 16-byte async copy
+// is aligned.  Block row J = rows [j0, j0+32):
+//   P = A[J, j0:] - U[0:j0, J]ᵀ U[0:j0, j0:]  (register tiles of 8×8, the
+//       finished rows of U streamed through shared memory 16 rows at a time
+//       with double-buffered cp.async), then the 32×32 diagonal block (one
+//       warp) and the TRSM of the rest of the block row.
+constexpr int kMxKChunk = 16;
+constexpr int kMxCChunk = 512;
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n"); }
+
+struct MxStage {
+  float p[2][kMxKChunk][kMxNB];
+  float c[2][kMxKChunk][kMxCChunk];
+};
+
+// Issue the async copies of U rows [k0, k0+kc) — columns [j0, j0+32) into
+// st.p[buf] and [j0+c0, j0+c0+wc) into st.c[buf] (wc rounded up to 4).
+__device__ __forceinline__ void mx_stage_issue(const float* U, int ldu, int j0, int c0, int wc4,
+                                               int k0, int kc, MxStage& st, int buf) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kc * (kMxNB / 4); e += blockDim.x) {
+    const int r = e / (kMxNB / 4), q = e % (kMxNB / 4);
+    cp_async16(&st.p[buf][r][4 * q], U + (int64_t)(k0 + r) * ldu + j0 + 4 * q);
+  }
+  const int per_row = wc4 >> 2;
+  for (int e = tid; e < kc * per_row; e += blockDim.x) {
+    const int r = e / per_row, q = e % per_row;
+    cp_async16(&st.c[buf][r][4 * q], U + (int64_t)(k0 + r) * ldu + j0 + c0 + 4 * q);
+  }
+  cp_async_commit();
+}
+
+__device__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
+                               MxStage& st) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ty = tid >> 6;   // 4 row groups of 8 rows
+  const int tx = tid & 63;   // 64 column groups of 8 contiguous columns
+  for (int j0 = 0; j0 < n; j0 += kMxNB) {
+    const int nb = min(kMxNB, n - j0);
+    const int W = n - j0;
+    for (int c0 = 0; c0 < W; c0 += kMxCChunk) {
+      const int wc = min(kMxCChunk, W - c0);
+      const int wc4 = min((wc + 3) & ~3, ldu - j0 - c0);
+      float acc[8][8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int p = 8 * ty + r;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = c0 + 8 * tx + q;
+          acc[r][q] = (p < nb && c < W) ? to_f32(A[(int64_t)(j0 + p) * n + j0 + c]) : 0.0f;
+        }
+      }
+      const int nchunks = (j0 + kMxKChunk - 1) / kMxKChunk;
+      if (nchunks > 0) mx_stage_issue(U, ldu, j0, c0, wc4, 0, min(kMxKChunk, j0), st, 0);
+      for (int ch = 0; ch < nchunks; ++ch) {
+        const int buf = ch & 1;
+        const int k0 = ch * kMxKChunk;
+        const int kc = min(kMxKChunk, j0 - k0);
+        if (ch + 1 < nchunks) {
+          mx_stage_issue(U, ldu, j0, c0, wc4, k0 + kMxKChunk, min(kMxKChunk, j0 - k0 - kMxKChunk),
+                         st, buf ^ 1);
+          cp_async_wait_one();
+        } else {
+          cp_async_wait_all();
+        }
+        __syncthreads();
+        if (8 * tx < wc) {
+          for (int kk = 0; kk < kc; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&st.p[buf][kk][8 * ty]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&st.p[buf][kk][8 * ty + 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&st.c[buf][kk][8 * tx]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&st.c[buf][kk][8 * tx + 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+              for (int q = 0; q < 8; ++q) acc[r][q] = fmaf(-av[r], bv[q], acc[r][q]);
+          }
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int p = 8 * ty + r;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = c0 + 8 * tx + q;
+          if (p < nb && c < W && c >= p) U[(int64_t)(j0 + p) * ldu + j0 + c] = acc[r][q];
+        }
+      }
+    }
+    __syncthreads();
+    // diagonal block by warp 0 in registers, then the block row TRSM
+    if (warp == 0) {
+      const int bad = warp_potrf_block<kMxNB>(U, ldu, j0, nb, sm.rd + j0);
+      if (lane == 0) sm.flag = bad;
+    }
+    __syncthreads();
+    if (sm.flag) return sm.flag;
+    block_row_trsm<kMxNB>(U, ldu, j0, nb, j0 + nb, n, sm.rd);
+    __syncthreads();
+  }
+  return 0;
+}
+
+// --- solves: (Uᵀ U) D = D for the live vectors of a chunk ------------------
+// U row stride ld (shared or global memory); D[c*n + i] in shared memory;
+// rd = 1/diag(U).  The warp solving a 32×32 diagonal block loads its column
+// (forward) or row (backward) of the block into registers first, so the
+// sequential steps only exchange values by shuffles; the off-diagonal
+// updates take one matrix row or column per thread for all NC vectors.
+template <int NC>
+__device__ void mx_solve_t(const float* U, int ld, int n, float* D, const float* rd,
+                           const MxSmem& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = blockDim.x >> 5;
+  const int nblk = (n + 31) >> 5;
+  for (int bi = 0; bi < nblk; ++bi) {  // forward: Uᵀ y = d
+    const int r0 = bi << 5, rn = min(32, n - r0);
+    for (int c = warp; c < NC; c += nw) {
+      if (sm.done[c]) continue;
+      float col[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) col[t] = (t < lane && lane < rn) ? U[(r0 + t) * ld + r0 + lane] : 0.0f;
+      const float rdl = (lane < rn) ? rd[r0 + lane] : 0.0f;
+      float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
+#pragma unroll
+      for (int t = 0; t < 32; ++t) {
+        if (t < rn) {
+          const float yt = __shfl_sync(0xffffffffu, v * rdl, t);
+          if (lane == t) v = yt;
+          else if (lane > t) v = fmaf(-col[t], yt, v);
+        }
+      }
+      if (lane < rn) D[c * n + r0 + lane] = v;
+    }
+    __syncthreads();
+    for (int i = r0 + rn + tid; i < n; i += blockDim.x) {
+      float v[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) v[c] = D[c * n + i];
+      for (int t = 0; t < rn; ++t) {
+        const float u = U[(r0 + t) * ld + i];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) D[c * n + i] = v[c];
+    }
+    __syncthreads();
+  }
+  for (int bi = nblk - 1; bi >= 0; --bi) {  // backward: U x = y
+    const int r0 = bi << 5, rn = min(32, n - r0);
+    for (int c = warp; c < NC; c += nw) {
+      if (sm.done[c]) continue;
+      float row[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) row[t] = (t > lane && t < rn) ? U[(r0 + lane) * ld + r0 + t] : 0.0f;
+      const float rdl = (lane < rn) ? rd[r0 + lane] : 0.0f;
+      float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
+#pragma unroll
+      for (int tt = 31; tt >= 0; --tt) {
+        if (tt < rn) {
+          const float xt = __shfl_sync(0xffffffffu, v * rdl, tt);
+          if (lane == tt) v = xt;
+          else if (lane < tt) v = fmaf(-row[tt], xt, v);
+        }
+      }
+      if (lane < rn) D[c * n + r0 + lane] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < r0; i += blockDim.x) {
+      const float* rowp = U + i * ld + r0;
+      float v[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) v[c] = D[c * n + i];
+      for (int t = 0; t < rn; ++t) {
+        const float u = rowp[t];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) D[c * n + i] = v[c];
+    }
+    __syncthreads();
+  }
+}
+
+// Split W FP64 values with one warp vote (see split_f64).
+template <int W>
+__device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], float (&lo)[W]) {
+  bool slow = false;
+#pragma unroll
+  for (int u = 0; u < W; ++u) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]);
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned mh = (unsigned)(b >> 29) & 0x7FFFFFu;
+    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;
+    const int sh = __clz(rem | 1u) - 8;
+    const unsigned m = (sh >= 0) ? (rem << sh) : (rem >> (-sh));
+    const int ex = (int)e - 1052 - sh + 127;
+    const bool zero = (b << 1) == 0ull;
+    hi[u] = zero ? __uint_as_float(sign) : __uint_as_float(sign | (((e - 1023u + 127u) & 0xFFu) << 23) | mh);
+    lo[u] = (rem == 0u) ? 0.0f : __uint_as_float(sign | (((unsigned)ex & 0xFFu) << 23) | (m & 0x7FFFFFu));
+    slow |= !zero && ((e < 949u) || (e > 1150u));
+  }
+  if (__any_sync(__activemask(), slow)) {
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a[u]) >> 52) & 0x7FFu;
+      if (a[u] != 0.0 && ((e < 949u) || (e > 1150u))) {
+        hi[u] = __double2float_rz(a[u]);
+        lo[u] = __double2float_rn(a[u] - (double)hi[u]);
+      }
+    }
+  }
+}
+
+// --- residual: D = fl32(B - A X) with X = XH + XL, FP64-accurate, no FP64 ops
+// A is split bitwise into hi+lo, hi*xh products made exact by an FMA
+// (TwoProd) and summed with TwoSum; ah*xl + al*xh, the product errors and the
+// summation errors go to a second FP32 accumulator.  b - Ax is formed in the
+// same double-float arithmetic from the split of b.  Lane c of each warp
+// finishes vector c.  Per-warp maxima of |r| and the row sums of |A| (for
+// ||A||_inf) land in sm.red / sm.red2.
+template <int NC>
+__device__ void mx_residual_t(const double* __restrict__ A, int n, const double* __restrict__ B,
+                              const float* XH, const float* XL, float* D, MxSmem& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  float rmax = 0.0f;   // lane c: max |r| of vector c
+  float rowmax = 0.0f;
+  for (int i = warp; i < n; i += nw) {
+    float S[NC], C[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) { S[c] = 0.0f; C[c] = 0.0f; }
+    float rs = 0.0f;
+    const double bval = (lane < NC) ? B[(int64_t)lane * n + i] : 0.0;
+    const double* row = A + (int64_t)i * n;
+    for (int j0 = 0; j0 < n; j0 += 256) {
+      double av[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + lane + 32 * u;
+        av[u] = (j < n) ? row[j] : 0.0;
+      }
+      float ah[8], al[8];
+      splitw<8>(av, ah, al);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + lane + 32 * u;
+        if (j < n) {
+          rs += fabsf(ah[u]);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            const float xh = XH[c * n + j], xl = XL[c * n + j];
+            const float p = ah[u] * xh;
+            const float pe = fmaf(ah[u], xh, -p);
+            float err;
+            two_sum(S[c], p, err);
+            C[c] += fmaf(ah[u], xl, fmaf(al[u], xh, pe + err));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      rs += __shfl_xor_sync(0xffffffffu, rs, o);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, S[c], o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, C[c], o);
+        float err;
+        two_sum(S[c], s2, err);
+        C[c] += c2 + err;
+      }
+    }
+    rowmax = fmaxf(rowmax, rs);
+    float Sl = 0.0f, Cl = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      if (lane == c) { Sl = S[c]; Cl = C[c]; }
+    if (lane < NC) {
+      float bh, bl;
+      split_f64(bval, bh, bl);
+      float rh = bh, re;
+      two_sum(rh, -Sl, re);
+      const float r = rh + ((bl - Cl) + re);
+      D[lane * n + i] = r;
+      rmax = fmaxf(rmax, fabsf(r));
+    }
+  }
+  if (lane < kMxKc) sm.red[warp][lane] = (lane < NC) ? rmax : 0.0f;
+  if (lane == 0) sm.red2[warp][0] = rowmax;
+}
+
+// x += d in double-float (TwoSum then Fast2Sum renormalisation) for live
+// vectors; per-warp max |x| into sm.red2[warp][1 + c].
+template <int NC>
+__device__ void mx_update_x(int n, const float* D, float* XH, float* XL, MxSmem& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float xm[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) xm[c] = 0.0f;
+  for (int i = tid; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (!sm.done[c]) {
+        float s = XH[c * n + i], e;
+        two_sum(s, D[c * n + i], e);
+        const float t = XL[c * n + i] + e;
+        const float h = s + t;
+        XH[c * n + i] = h;
+        XL[c * n + i] = t - (h - s);
+      }
+      xm[c] = fmaxf(xm[c], fabsf(XH[c * n + i]));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    float v = xm[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sm.red2[warp][1 + c] = v;
+  }
+}
+
+// One refinement chunk of NC vectors: solves, x updates and residuals until
+// every vector's backward error is <= tol or max_iter solves were applied.
+template <int NC>
+__device__ void mx_refine(const float* F, int ld, int n, const double* __restrict__ A,
+                          const double* __restrict__ B, double* __restrict__ X, float* D,
+                          float* XH, float* XL, double tol, int max_iter, bool& first_residual,
+                          int& iters_out, bool& converged, MxSmem& sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  if (tid < kMxKc) { sm.done[tid] = 0; sm.berr[tid] = 0.0; }
+  // d = fl32(b), x = 0, ||b||_inf
+  float bm[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) bm[c] = 0.0f;
+  for (int i = tid; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const float v = to_f32(B[(int64_t)c * n + i]);
+      D[c * n + i] = v;
+      XH[c * n + i] = 0.0f;
+      XL[c * n + i] = 0.0f;
+      bm[c] = fmaxf(bm[c], fabsf(v));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    float v = bm[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sm.red[warp][c] = v;
   }
   __syncthreads();
-  if (threadIdx.x < nc) {
-    double xm = 0.0;
-    for (int w = 0; w < nw; ++w) xm = fmax(xm, sm.red[w][threadIdx.x]);
-    const double den = sm.anorm * xm + sm.bnorm[threadIdx.x];
-    const double num = sm.berr[threadIdx.x];
-    sm.berr[threadIdx.x] = (den > 0.0) ? num / den : (num > 0.0 ? INFINITY : 0.0);
+  if (tid < NC) {
+    float m = 0.0f;
+    for (int w = 0; w < nw; ++w) m = fmaxf(m, sm.red[w][tid]);
+    sm.bnorm[tid] = m;
   }
+  __syncthreads();
+  int it = 0;
+  bool all_done = false;
+  for (;;) {
+    mx_solve_t<NC>(F, ld, n, D, sm.rd, sm);
+    mx_update_x<NC>(n, D, XH, XL, sm);
+    ++it;
+    __syncthreads();
+    mx_residual_t<NC>(A, n, B, XH, XL, D, sm);
+    __syncthreads();
+    if (tid == 0) {
+      if (first_residual) {
+        float m = 0.0f;
+        for (int w = 0; w < nw; ++w) m = fmaxf(m, sm.red2[w][0]);
+        sm.anorm = m;
+      }
+      int all = 1;
+      for (int c = 0; c < NC; ++c) {
+        if (!sm.done[c]) {
+          float rm = 0.0f, xm = 0.0f;
+          for (int w = 0; w < nw; ++w) {
+            rm = fmaxf(rm, sm.red[w][c]);
+            xm = fmaxf(xm, sm.red2[w][1 + c]);
+          }
+          const double den = (double)sm.anorm * (double)xm + (double)sm.bnorm[c];
+          const double be = (den > 0.0) ? (double)rm / den : (rm > 0.0f ? INFINITY : 0.0);
+          sm.berr[c] = be;
+          if (be <= tol) sm.done[c] = 1;
+        }
+        if (!sm.done[c]) all = 0;
+      }
+      sm.flag = all;
+    }
+    first_residual = false;
+    __syncthreads();
+    all_done = sm.flag != 0;
+    if (all_done || it >= max_iter) break;
+  }
+  // x out in FP64
+  for (int i = tid; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      X[(int64_t)c * n + i] = (double)XH[c * n + i] + (double)XL[c * n + i];
+  }
+  iters_out = it;
+  converged = all_done;
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kCholThreads)
+__device__ __forceinline__ int mx_next(int* queue, int* s_next) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_next = atomicAdd(queue, 1);
+  __syncthreads();
+  return *s_next;
+}
+
+__global__ void __launch_bounds__(kMxThreads, 2)
 posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restrict__ nvec,
                   const int32_t* __restrict__ nrhs_vec, const int64_t* __restrict__ a_off,
                   const double* __restrict__ a, const int64_t* __restrict__ b_off,
                   const double* __restrict__ b, double* __restrict__ x, double tol, int max_iter,
                   int32_t* __restrict__ info, int32_t* __restrict__ iters,
                   double* __restrict__ berr_out, int* queue, float* __restrict__ factor_ws) {
-  extern __shared__ float smem_mixed[];
-  __shared__ MixedSmem sm;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  extern __shared__ float smem_mx[];
+  __shared__ MxSmem sm;
+  const int tid = threadIdx.x;
   for (;;) {
-    const int s = next_system(queue, &sm.next);
+    const int s = mx_next(queue, &sm.next);
     if (s >= batch) break;
     const int n = nvec[s];
     const int nrhs = nrhs_vec[s];
@@ -269,34 +834,32 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
       if (tid == 0) { info[s] = -2; iters[s] = 0; berr_out[s] = NAN; }
       continue;
     }
+    if (n == 0) {
+      if (tid == 0) { info[s] = 0; iters[s] = 0; berr_out[s] = 0.0; }
+      continue;
+    }
     const double* A = a + a_off[s];
-    const bool in_smem = n <= kCholSmemMaxF32;
-    const int ld = in_smem ? (n | 1) : n;
-    float* F = in_smem ? smem_mixed : factor_ws + (int64_t)blockIdx.x * max_n * max_n;
-    float* d = in_smem ? smem_mixed + n * ld : smem_mixed;  // correction vectors
-    const int ldd = n;
-    // Load the upper triangle in FP32 and form ||A||_inf in FP64 from the
-    // full stored matrix (the operator whose residual is refined).
-    double rowmax = 0.0;
-    for (int i = warp; i < n; i += nw) {
-      double rs = 0.0;
-      for (int j = lane; j < n; j += 32) {
-        const double v = A[(int64_t)i * n + j];
-        rs += fabs(v);
-        if (j >= i) F[i * ld + j] = (float)v;
+    const bool small = n <= kMxSmallN;
+    const int ld = small ? (n | 1) : ((n + 31) & ~31);
+    const int ldmax = (max_n + 31) & ~31;
+    float* F = small ? smem_mx : factor_ws + (int64_t)blockIdx.x * ldmax * ldmax;
+    float* vec = small ? smem_mx + n * ld : smem_mx;   // D | XH | XL, kMxKc*n each
+    float* D = vec;
+    float* XH = vec + kMxKc * n;
+    float* XL = vec + 2 * kMxKc * n;
+    if (tid == 0) sm.flag = 0;
+    int rc;
+    if (small) {
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e - i * n;
+        if (j >= i) F[i * ld + j] = to_f32(A[e]);
       }
-      rs = warp_sum(rs);
-      rowmax = fmax(rowmax, rs);
+      __syncthreads();
+      rc = mx_factor_small(F, ld, n, sm);
+    } else {
+      __syncthreads();
+      rc = mx_factor_large(A, F, n, ld, sm, *reinterpret_cast<MxStage*>(smem_mx));
     }
-    if (lane == 0) sm.red[warp][0] = rowmax;
-    __syncthreads();
-    if (tid == 0) {
-      double m = 0.0;
-      for (int w = 0; w < nw; ++w) m = fmax(m, sm.red[w][0]);
-      sm.anorm = m;
-    }
-    __syncthreads();
-    int rc = in_smem ? cta_potrf_upper<float, 16>(F, ld, n) : cta_potrf_upper<float, 32>(F, ld, n);
     __syncthreads();
     if (rc != 0) {
       for (int e = tid; e < n * nrhs; e += blockDim.x) x[b_off[s] + e] = NAN;
@@ -304,63 +867,29 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
       continue;
     }
     double sys_berr = 0.0;
-    int sys_iters = 0;
-    int sys_info = 0;
-    for (int c0 = 0; c0 < nrhs; c0 += kMixedRhsChunk) {
-      const int nc = min(kMixedRhsChunk, nrhs - c0);
+    int sys_iters = 0, sys_info = 0;
+    bool first = true;
+    for (int c0 = 0; c0 < nrhs; c0 += kMxKc) {
+      const int nc = min(kMxKc, nrhs - c0);
       const double* B = b + b_off[s] + (int64_t)c0 * n;
       double* X = x + b_off[s] + (int64_t)c0 * n;
-      // x = 0, d = (float) b, ||b||_inf
-      if (tid < nc) { sm.done[tid] = 0; sm.bnorm[tid] = 0.0; }
-      __syncthreads();
-      for (int c = 0; c < nc; ++c) {
-        double bm = 0.0;
-        for (int i = tid; i < n; i += blockDim.x) {
-          const double v = B[(int64_t)c * n + i];
-          X[(int64_t)c * n + i] = 0.0;
-          d[c * ldd + i] = (float)v;
-          bm = fmax(bm, fabs(v));
-        }
-        bm = warp_max(bm);
-        if (lane == 0) sm.red[warp][c] = bm;
-      }
-      __syncthreads();
-      if (tid < nc) {
-        double m = 0.0;
-        for (int w = 0; w < nw; ++w) m = fmax(m, sm.red[w][tid]);
-        sm.bnorm[tid] = m;
-      }
-      __syncthreads();
       int it = 0;
-      for (;;) {
-        // correction solves with the FP32 factor, for vectors not yet done
-        for (int c = 0; c < nc; ++c) {
-          if (sm.done[c]) continue;  // uniform: shared value read after a barrier
-          cta_trsv<float>(F, ld, n, /*lower=*/false, /*trans=*/true, /*unit=*/false, d + c * ldd, sm.tsm);
-          cta_trsv<float>(F, ld, n, /*lower=*/false, /*trans=*/false, /*unit=*/false, d + c * ldd, sm.tsm);
-        }
-        for (int c = 0; c < nc; ++c) {
-          if (sm.done[c]) continue;
-          for (int i = tid; i < n; i += blockDim.x) X[(int64_t)c * n + i] += (double)d[c * ldd + i];
-        }
-        ++it;
-        __syncthreads();
-        residual_f64(A, n, B, X, nc, d, ldd, sm);
-        if (tid == 0) {
-          int all = 1;
-          for (int c = 0; c < nc; ++c) {
-            if (!(sm.berr[c] <= tol) && !sm.done[c]) all = 0;
-            if (sm.berr[c] <= tol) sm.done[c] = 1;
-          }
-          sm.all_done = all;
-        }
-        __syncthreads();
-        if (sm.all_done || it >= max_iter) break;
+      bool conv = true;
+      switch (nc) {
+        case 1: mx_refine<1>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 2: mx_refine<2>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 3: mx_refine<3>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 4: mx_refine<4>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 5: mx_refine<5>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 6: mx_refine<6>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        case 7: mx_refine<7>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
+        default: mx_refine<8>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
       }
-      if (!sm.all_done) sys_info = -1;
+      if (!conv) sys_info = -1;
       for (int c = 0; c < nc; ++c) sys_berr = fmax(sys_berr, sm.berr[c]);
       sys_iters = max(sys_iters, it);
       __syncthreads();
+      if (tid == 0) sm.flag = 0;
     }
     if (tid == 0) { info[s] = sys_info; iters[s] = sys_iters; berr_out[s] = sys_berr; }
   }
@@ -368,17 +897,44 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
 
 __global__ void reset_queue_kernel(int* queue) { *queue = 0; }
 
+static size_t mixed_smem_bytes(int max_n, int max_nrhs) {
+  (void)max_nrhs;
+  const int ns = max_n < kMxSmallN ? max_n : kMxSmallN;
+  const size_t small = (size_t)ns * (ns | 1) * sizeof(float) + (size_t)3 * kMxKc * ns * sizeof(float);
+  size_t large = (size_t)3 * kMxKc * max_n * sizeof(float);
+  if (max_n > kMxSmallN && large < sizeof(MxStage)) large = sizeof(MxStage);
+  return small > large ? small : large;
+}
+
+// Workspace: queue header + one FP32 max_n² factor slice per CTA when some
+// system can exceed the shared-memory size.
+static int64_t mixed_slice_bytes(int max_n) {
+  const int64_t ld = (max_n + 31) & ~31;
+  return (max_n > kMxSmallN) ? ld * ld * (int64_t)sizeof(float) : 0;
+}
+
 static int mixed_grid(int64_t batch) {
-  const int64_t g = sm_count();
+  const int64_t g = 2LL * sm_count();
   return (int)((batch < g) ? batch : g);
 }
 
-static size_t mixed_smem_bytes(int max_n, int max_nrhs) {
-  const int nc = max_nrhs < kMixedRhsChunk ? max_nrhs : kMixedRhsChunk;
-  const int ns = max_n < kCholSmemMaxF32 ? max_n : kCholSmemMaxF32;
-  size_t small = (size_t)ns * (ns | 1) * sizeof(float) + (size_t)ns * nc * sizeof(float);
-  size_t large = (size_t)max_n * nc * sizeof(float);
-  return small > large ? small : large;
+// Launch over `grid` CTAs with the given scratch (queue + factor slices).
+static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs, const int32_t* n,
+                        const int32_t* nrhs, const int64_t* a_off, const double* a,
+                        const int64_t* b_off, const double* b, double* x, double tol,
+                        int32_t max_iter, int32_t* info, int32_t* iters, double* berr,
+                        void* scratch, cudaStream_t st) {
+  int* queue = reinterpret_cast<int*>(scratch);
+  float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + kQueueHeader);
+  reset_queue_kernel<<<1, 1, 0, st>>>(queue);
+  const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
+  LXGB_CUDA_TRY(cudaFuncSetAttribute(posv_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem),
+                "posv_mixed: set smem");
+  posv_mixed_kernel<<<(unsigned)grid, kMxThreads, smem, st>>>(
+      batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
+      queue, factor_ws);
+  return check_launch("posv_mixed");
 }
 
 }  // namespace lxgb
@@ -425,10 +981,7 @@ extern "C" int64_t lxgb_posv_ragged_mixed_workspace_size(int64_t batch, int32_t 
                                                          int32_t max_nrhs) {
   (void)max_nrhs;
   if (batch <= 0 || max_n <= 0) return kQueueHeader;
-  int64_t bytes = kQueueHeader;
-  if (max_n > kCholSmemMaxF32)
-    bytes += (int64_t)mixed_grid(batch) * max_n * max_n * (int64_t)sizeof(float);
-  return bytes;
+  return kQueueHeader + (int64_t)mixed_grid(batch) * mixed_slice_bytes(max_n);
 }
 
 extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
@@ -443,24 +996,14 @@ extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_
   LXGB_REQUIRE(n && nrhs && a_off && a && b_off && b && x && info && iters && berr && work,
                "posv_mixed: null pointer");
   LXGB_REQUIRE(max_iter >= 1, "posv_mixed: max_iter must be >= 1");
+  LXGB_REQUIRE(max_n <= kMxMaxN, "posv_mixed: max_n above 1024");
   LXGB_REQUIRE(((uintptr_t)work & 255) == 0, "posv_mixed: workspace must be 256-byte aligned");
   if (work_bytes < lxgb_posv_ragged_mixed_workspace_size(batch, max_n, max_nrhs)) {
     set_last_error("posv_mixed: workspace too small");
     return LXGB_WORKSPACE_TOO_SMALL;
   }
-  cudaStream_t st = as_stream(stream);
-  int* queue = reinterpret_cast<int*>(work);
-  float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(work) + kQueueHeader);
-  reset_queue_kernel<<<1, 1, 0, st>>>(queue);
-  const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
-  LXGB_REQUIRE(max_n <= kMixedMaxN, "posv_mixed: max_n above 2048");
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(posv_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem),
-                "posv_mixed: set smem");
-  posv_mixed_kernel<<<(unsigned)mixed_grid(batch), kCholThreads, smem, st>>>(
-      batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
-      queue, factor_ws);
-  return check_launch("posv_mixed");
+  return mixed_launch(mixed_grid(batch), batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x,
+                      tol, max_iter, info, iters, berr, work, as_stream(stream));
 }
 
 // ---------------------------------------------------------------------------
@@ -519,14 +1062,13 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
   LXGB_REQUIRE(n && nrhs && a_off && a && b_off && b && x && info && iters && berr,
                "posv_mixed_noalloc: null pointer");
   LXGB_REQUIRE(max_iter >= 1, "posv_mixed_noalloc: max_iter must be >= 1");
-  LXGB_REQUIRE(max_n <= kMixedMaxN,
-               "posv_mixed_noalloc: max_n above 2048 (its FP32 factor exceeds the fixed scratch)");
+  LXGB_REQUIRE(max_n <= kMxMaxN,
+               "posv_mixed_noalloc: max_n above 1024");
   // Grid: one FP32 factor slice per CTA for systems above the shared-memory
   // size, as many slices as the fixed scratch holds.
-  int64_t grid = sm_count();
-  if (batch < grid) grid = batch;
-  if (max_n > kCholSmemMaxF32) {
-    const int64_t slice = (int64_t)max_n * max_n * (int64_t)sizeof(float);
+  int64_t grid = mixed_grid(batch);
+  const int64_t slice = mixed_slice_bytes(max_n);
+  if (slice > 0) {
     const int64_t slices = (int64_t)(LXGB_POSV_NOALLOC_SCRATCH_BYTES - kQueueHeader) / slice;
     if (slices < 1) {
       set_last_error("posv_mixed_noalloc: max_n=%d needs %lld bytes of scratch, limit %lld", max_n,
@@ -539,16 +1081,8 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
   void* scratch = nullptr;
   int rc = noalloc_scratch_address(&scratch);
   if (rc) return rc;
-  cudaStream_t st = as_stream(stream);
-  int* queue = reinterpret_cast<int*>(scratch);
-  float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + kQueueHeader);
-  reset_queue_kernel<<<1, 1, 0, st>>>(queue);  // the array keeps the previous call's counter
-  const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(posv_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem),
-                "posv_mixed_noalloc: set smem");
-  posv_mixed_kernel<<<(unsigned)grid, kCholThreads, smem, st>>>(
-      batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
-      queue, factor_ws);
-  return check_launch("posv_mixed_noalloc");
+  // mixed_launch clears the work-queue counter, which the array keeps from the
+  // previous call.
+  return mixed_launch((int)grid, batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol,
+                      max_iter, info, iters, berr, scratch, as_stream(stream));
 }
