@@ -205,6 +205,8 @@ constexpr int kMxMaxN = 1024;
 
 struct MxSmem {
   float rd[kMxMaxN];                     // 1 / diagonal of the FP32 factor
+  float ublk[kMxNB][kMxNB + 1];          // the current diagonal block of U
+  float linv[kMxNB][kMxNB + 1];          // its inverse transpose, U_JJ^{-T} (lower)
   float red[kMxThreads / 32][kMxKc];     // per-warp partial maxima
   float red2[kMxThreads / 32][kMxKc + 1];  // [0]: row-sum max, [1 + c]: max |x_c|
   float anorm;
@@ -260,84 +262,96 @@ __device__ __forceinline__ void two_sum(float& s, float t, float& err) {
 // Factor the nb×nb diagonal block at F[j0.., j0..] (upper triangle, row
 // stride ld) by one warp entirely in registers: lane j holds column j; row k
 // of U is formed in place and rows i > k updated with u_ki fetched by shuffle.
-// Writes U_JJ back and 1/diag into rd[0..nb).  Returns 0 or (j0+k+1) for the
-// first pivot that is not positive.
+// The block is padded to NBMAX with the identity, so every step runs
+// unconditionally (shuffles outside data-dependent branches); a pivot that is
+// not positive is recorded, not branched on.  Writes U_JJ back to F and to
+// ublk (NBMAX×(NBMAX+1) shared array) and 1/diag into rd[0..nb).  Returns 0 or
+// (j0+k+1) for the first pivot that is not positive.
 template <int NBMAX>
-__device__ int warp_potrf_block(float* F, int64_t ld, int j0, int nb, float* rd) {
+__device__ __noinline__ int warp_potrf_block(float* F, int64_t ld, int j0, int nb, float* rd, float* ublk,
+                                             float* linv) {
   const int lane = threadIdx.x & 31;
   float col[NBMAX];
 #pragma unroll
-  for (int i = 0; i < NBMAX; ++i)
-    col[i] = (i < nb && i <= lane && lane < nb) ? F[(int64_t)(j0 + i) * ld + j0 + lane] : 0.0f;
+  for (int i = 0; i < NBMAX; ++i) {
+    const bool in = (i < nb) && (i <= lane) && (lane < nb);
+    col[i] = in ? F[(int64_t)(j0 + i) * ld + j0 + lane] : ((i == lane) ? 1.0f : 0.0f);
+  }
   int bad = 0;
 #pragma unroll
   for (int k = 0; k < NBMAX; ++k) {
-    if (k < nb && bad == 0) {
-      const float akk = __shfl_sync(0xffffffffu, col[k], k);
-      if (!(akk > 0.0f)) {
-        bad = j0 + k + 1;
-      } else {
-        const float d = sqrtf(akk);
-        const float r = 1.0f / d;
-        if (lane == k) col[k] = d;
-        else if (lane > k) col[k] *= r;
-        if (lane == 0) rd[k] = r;
+    const float akk = __shfl_sync(0xffffffffu, col[k], k);
+    if (!(akk > 0.0f) && bad == 0) bad = j0 + k + 1;
+    const float d = sqrtf(akk);
+    const float r = 1.0f / d;
+    col[k] = (lane == k) ? d : ((lane > k) ? col[k] * r : col[k]);
+    if (lane == 0 && k < nb) rd[k] = r;
 #pragma unroll
-        for (int i = k + 1; i < NBMAX; ++i) {
-          if (i < nb) {
-            const float uki = __shfl_sync(0xffffffffu, col[k], i);
-            if (lane >= i) col[i] = fmaf(-uki, col[k], col[i]);
-          }
-        }
-      }
+    for (int i = k + 1; i < NBMAX; ++i) {
+      const float uki = __shfl_sync(0xffffffffu, col[k], i);
+      col[i] = (lane >= i) ? fmaf(-uki, col[k], col[i]) : col[i];
     }
   }
-  if (bad == 0) {
 #pragma unroll
-    for (int i = 0; i < NBMAX; ++i)
-      if (i < nb && i <= lane && lane < nb) F[(int64_t)(j0 + i) * ld + j0 + lane] = col[i];
+  for (int i = 0; i < NBMAX; ++i) {
+    if (lane < NBMAX) ublk[i * (NBMAX + 1) + lane] = col[i];
+    if (bad == 0 && i < nb && i <= lane && lane < nb) F[(int64_t)(j0 + i) * ld + j0 + lane] = col[i];
   }
+  __syncwarp();
+  // Linv = U_JJ^{-T}: lane j solves U_JJᵀ z = e_j (z[p] = 0 for p < j) and
+  // stores z as column j of Linv.
+  if (lane < NBMAX) {
+    float z[NBMAX];
+#pragma unroll
+    for (int p = 0; p < NBMAX; ++p) {
+      float v = (p == lane) ? 1.0f : 0.0f;
+#pragma unroll
+      for (int q = 0; q < p; ++q) v = fmaf(-ublk[q * (NBMAX + 1) + p], z[q], v);
+      z[p] = v / ublk[p * (NBMAX + 1) + p];
+    }
+#pragma unroll
+    for (int p = 0; p < NBMAX; ++p) linv[p * (NBMAX + 1) + lane] = z[p];
+  }
+  __syncwarp();
   return bad;
 }
 
 // Rows [kb, kb+nb) of the block row: U[kb:kb+nb, j] = U_kk^{-T} A[kb:kb+nb, j]
-// for columns j in [j_lo, n), one column per thread.
+// for columns j in [j_lo, n), one column per thread, as a triangular
+// matrix-vector product with Linv = U_kk^{-T} (shared): each output row is
+// formed and stored at once, keeping register pressure at one column.
 template <int NBMAX>
-__device__ void block_row_trsm(float* F, int64_t ld, int kb, int nb, int j_lo, int n,
-                               const float* rd) {
+__device__ __noinline__ void block_row_trsm(float* F, int64_t ld, int kb, int nb, int j_lo, int n,
+                                            const float* linv) {
   for (int j = j_lo + threadIdx.x; j < n; j += blockDim.x) {
-    float y[NBMAX];
+    float a[NBMAX];
 #pragma unroll
-    for (int p = 0; p < NBMAX; ++p) y[p] = (p < nb) ? F[(int64_t)(kb + p) * ld + j] : 0.0f;
+    for (int p = 0; p < NBMAX; ++p) a[p] = (p < nb) ? F[(int64_t)(kb + p) * ld + j] : 0.0f;
 #pragma unroll
     for (int p = 0; p < NBMAX; ++p) {
-      if (p < nb) {
-        float v = y[p];
+      float y = 0.0f;
 #pragma unroll
-        for (int q = 0; q < p; ++q) v = fmaf(-F[(int64_t)(kb + q) * ld + kb + p], y[q], v);
-        y[p] = v * rd[kb + p];
-      }
+      for (int q = 0; q <= p; ++q) y = fmaf(linv[p * (NBMAX + 1) + q], a[q], y);
+      if (p < nb) F[(int64_t)(kb + p) * ld + j] = y;
     }
-#pragma unroll
-    for (int p = 0; p < NBMAX; ++p)
-      if (p < nb) F[(int64_t)(kb + p) * ld + j] = y[p];
   }
 }
 
 // --- small path: right-looking in shared memory ---------------------------
 // Returns 0 or k+1.  F row stride ld, upper triangle.
-__device__ int mx_factor_small(float* F, int ld, int n, MxSmem& sm) {
+__device__ __noinline__ int mx_factor_small(float* F, int ld, int n, MxSmem& sm) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int tx = tid & 15, ty = tid >> 4;
   for (int kb = 0; kb < n; kb += 16) {
     const int ke = min(kb + 16, n);
     if (warp == 0) {
-      const int bad = warp_potrf_block<16>(F, ld, kb, ke - kb, sm.rd + kb);
+      const int bad = warp_potrf_block<16>(F, ld, kb, ke - kb, sm.rd + kb, &sm.ublk[0][0],
+                                           &sm.linv[0][0]);
       if ((tid & 31) == 0) sm.flag = bad;
     }
     __syncthreads();
     if (sm.flag) return sm.flag;
-    block_row_trsm<16>(F, ld, kb, ke - kb, ke, n, sm.rd);
+    block_row_trsm<16>(F, ld, kb, ke - kb, ke, n, &sm.linv[0][0]);
     __syncthreads();
     // trailing update of [ke, n): F[i][j] -= sum_p F[p][i] F[p][j], j >= i
     const int m = n - ke;
@@ -386,116 +400,98 @@ __device__ int mx_factor_small(float* F, int ld, int n, MxSmem& sm) {
   return 0;
 }
 
-// --- large path: left-looking by 32-row block rows, U in global -----------
-// U has row stride ldu (n rounded up to 32) so that every 16-byte async copy
-// is aligned.  Block row J = rows [j0, j0+32):
-//   P = A[J, j0:] - U[0:j0, J]ᵀ U[0:j0, j0:]  (register tiles of 8×8, the
-//       finished rows of U streamed through shared memory 16 rows at a time
-//       with double-buffered cp.async), then the 32×32 diagonal block (one
-//       warp) and the TRSM of the rest of the block row.
-constexpr int kMxKChunk = 16;
-constexpr int kMxCChunk = 512;
-
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n"); }
+// --- large path: right-looking by 32-row block rows, U in global ----------
+// U (row stride ldu = n rounded up to 32, so 8-float tiles stay inside the
+// row) first receives the upper triangle of A in FP32.  Per block row J:
+// the diagonal block by one warp in registers, the TRSM of the rest of the
+// block row (U_JJ from shared memory), the block row staged in shared memory
+// (up to kMxStageCols columns), then the trailing update of the upper
+// triangle in 8×8 register tiles, U[i][j] -= sum_p U[p][i] U[p][j].
+constexpr int kMxStageCols = 512;
 
 struct MxStage {
-  float p[2][kMxKChunk][kMxNB];
-  float c[2][kMxKChunk][kMxCChunk];
+  float brow[kMxNB][kMxStageCols];
 };
 
-// Issue the async copies of U rows [k0, k0+kc) — columns [j0, j0+32) into
-// st.p[buf] and [j0+c0, j0+c0+wc) into st.c[buf] (wc rounded up to 4).
-__device__ __forceinline__ void mx_stage_issue(const float* U, int ldu, int j0, int c0, int wc4,
-                                               int k0, int kc, MxStage& st, int buf) {
-  const int tid = threadIdx.x;
-  for (int e = tid; e < kc * (kMxNB / 4); e += blockDim.x) {
-    const int r = e / (kMxNB / 4), q = e % (kMxNB / 4);
-    cp_async16(&st.p[buf][r][4 * q], U + (int64_t)(k0 + r) * ldu + j0 + 4 * q);
-  }
-  const int per_row = wc4 >> 2;
-  for (int e = tid; e < kc * per_row; e += blockDim.x) {
-    const int r = e / per_row, q = e % per_row;
-    cp_async16(&st.c[buf][r][4 * q], U + (int64_t)(k0 + r) * ldu + j0 + c0 + 4 * q);
-  }
-  cp_async_commit();
-}
-
-__device__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
+__device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
                                MxStage& st) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ty = tid >> 6;   // 4 row groups of 8 rows
-  const int tx = tid & 63;   // 64 column groups of 8 contiguous columns
+  // FP32 copy of the upper triangle
+  for (int i = warp; i < n; i += blockDim.x >> 5)
+    for (int j = i + lane; j < n; j += 32) U[(int64_t)i * ldu + j] = to_f32(A[(int64_t)i * n + j]);
+  __syncthreads();
   for (int j0 = 0; j0 < n; j0 += kMxNB) {
     const int nb = min(kMxNB, n - j0);
-    const int W = n - j0;
-    for (int c0 = 0; c0 < W; c0 += kMxCChunk) {
-      const int wc = min(kMxCChunk, W - c0);
-      const int wc4 = min((wc + 3) & ~3, ldu - j0 - c0);
-      float acc[8][8];
-#pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const int p = 8 * ty + r;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int c = c0 + 8 * tx + q;
-          acc[r][q] = (p < nb && c < W) ? to_f32(A[(int64_t)(j0 + p) * n + j0 + c]) : 0.0f;
-        }
-      }
-      const int nchunks = (j0 + kMxKChunk - 1) / kMxKChunk;
-      if (nchunks > 0) mx_stage_issue(U, ldu, j0, c0, wc4, 0, min(kMxKChunk, j0), st, 0);
-      for (int ch = 0; ch < nchunks; ++ch) {
-        const int buf = ch & 1;
-        const int k0 = ch * kMxKChunk;
-        const int kc = min(kMxKChunk, j0 - k0);
-        if (ch + 1 < nchunks) {
-          mx_stage_issue(U, ldu, j0, c0, wc4, k0 + kMxKChunk, min(kMxKChunk, j0 - k0 - kMxKChunk),
-                         st, buf ^ 1);
-          cp_async_wait_one();
-        } else {
-          cp_async_wait_all();
-        }
-        __syncthreads();
-        if (8 * tx < wc) {
-          for (int kk = 0; kk < kc; ++kk) {
-            const float4 a0 = *reinterpret_cast<const float4*>(&st.p[buf][kk][8 * ty]);
-            const float4 a1 = *reinterpret_cast<const float4*>(&st.p[buf][kk][8 * ty + 4]);
-            const float4 b0 = *reinterpret_cast<const float4*>(&st.c[buf][kk][8 * tx]);
-            const float4 b1 = *reinterpret_cast<const float4*>(&st.c[buf][kk][8 * tx + 4]);
-            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-#pragma unroll
-              for (int q = 0; q < 8; ++q) acc[r][q] = fmaf(-av[r], bv[q], acc[r][q]);
-          }
-        }
-        __syncthreads();
-      }
-#pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const int p = 8 * ty + r;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int c = c0 + 8 * tx + q;
-          if (p < nb && c < W && c >= p) U[(int64_t)(j0 + p) * ldu + j0 + c] = acc[r][q];
-        }
-      }
-    }
-    __syncthreads();
-    // diagonal block by warp 0 in registers, then the block row TRSM
     if (warp == 0) {
-      const int bad = warp_potrf_block<kMxNB>(U, ldu, j0, nb, sm.rd + j0);
+      const int bad = warp_potrf_block<kMxNB>(U, ldu, j0, nb, sm.rd + j0, &sm.ublk[0][0],
+                                              &sm.linv[0][0]);
       if (lane == 0) sm.flag = bad;
     }
     __syncthreads();
     if (sm.flag) return sm.flag;
-    block_row_trsm<kMxNB>(U, ldu, j0, nb, j0 + nb, n, sm.rd);
+    const int t0 = j0 + nb;          // first trailing row/column
+    const int m = n - t0;            // trailing order
+    if (m <= 0) break;
+    block_row_trsm<kMxNB>(U, ldu, j0, nb, t0, n, &sm.linv[0][0]);
+    __syncthreads();
+    const bool staged = m <= kMxStageCols;
+    if (staged) {
+      const int m4 = (m + 3) >> 2;
+      for (int e = tid; e < kMxNB * m4; e += blockDim.x) {
+        const int p = e / m4, q = e % m4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p < nb) v = *reinterpret_cast<const float4*>(U + (int64_t)(j0 + p) * ldu + t0 + 4 * q);
+        *reinterpret_cast<float4*>(&st.brow[p][4 * q]) = v;
+      }
+      __syncthreads();
+    }
+    // 8×8 tiles of the upper triangle of the trailing matrix
+    const int mt = (m + 7) >> 3;
+    const int ntiles = mt * (mt + 1) / 2;
+    for (int t = tid; t < ntiles; t += blockDim.x) {
+      // (ti, tj) with tj >= ti from the linear index over the triangle
+      int ti = (int)((2.0f * mt + 1.0f - sqrtf((2.0f * mt + 1.0f) * (2.0f * mt + 1.0f) - 8.0f * t)) * 0.5f);
+      while (ti > 0 && ti * (2 * mt - ti + 1) / 2 > t) --ti;
+      while ((ti + 1) * (2 * mt - ti) / 2 <= t) ++ti;
+      const int tj = ti + (t - ti * (2 * mt - ti + 1) / 2);
+      const int ri = ti << 3, cj = tj << 3;   // offsets inside the trailing matrix
+      float acc[8][8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const float* src = U + (int64_t)(t0 + ri + r) * ldu + t0 + cj;
+        const float4 a0 = *reinterpret_cast<const float4*>(src);
+        const float4 a1 = *reinterpret_cast<const float4*>(src + 4);
+        acc[r][0] = a0.x; acc[r][1] = a0.y; acc[r][2] = a0.z; acc[r][3] = a0.w;
+        acc[r][4] = a1.x; acc[r][5] = a1.y; acc[r][6] = a1.z; acc[r][7] = a1.w;
+      }
+      for (int p = 0; p < nb; ++p) {
+        float ai[8], bj[8];
+        if (staged) {
+          const float4 x0 = *reinterpret_cast<const float4*>(&st.brow[p][ri]);
+          const float4 x1 = *reinterpret_cast<const float4*>(&st.brow[p][ri + 4]);
+          const float4 y0 = *reinterpret_cast<const float4*>(&st.brow[p][cj]);
+          const float4 y1 = *reinterpret_cast<const float4*>(&st.brow[p][cj + 4]);
+          ai[0] = x0.x; ai[1] = x0.y; ai[2] = x0.z; ai[3] = x0.w;
+          ai[4] = x1.x; ai[5] = x1.y; ai[6] = x1.z; ai[7] = x1.w;
+          bj[0] = y0.x; bj[1] = y0.y; bj[2] = y0.z; bj[3] = y0.w;
+          bj[4] = y1.x; bj[5] = y1.y; bj[6] = y1.z; bj[7] = y1.w;
+        } else {
+          const float* rowp = U + (int64_t)(j0 + p) * ldu + t0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) { ai[q] = rowp[ri + q]; bj[q] = rowp[cj + q]; }
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[r][q] = fmaf(-ai[r], bj[q], acc[r][q]);
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        float* dst = U + (int64_t)(t0 + ri + r) * ldu + t0 + cj;
+        *reinterpret_cast<float4*>(dst) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+        *reinterpret_cast<float4*>(dst + 4) = make_float4(acc[r][4], acc[r][5], acc[r][6], acc[r][7]);
+      }
+    }
     __syncthreads();
   }
   return 0;
@@ -508,7 +504,7 @@ __device__ int mx_factor_large(const double* __restrict__ A, float* U, int n, in
 // sequential steps only exchange values by shuffles; the off-diagonal
 // updates take one matrix row or column per thread for all NC vectors.
 template <int NC>
-__device__ void mx_solve_t(const float* U, int ld, int n, float* D, const float* rd,
+__device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, float* D, const float* rd,
                            const MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nw = blockDim.x >> 5;
@@ -523,12 +519,9 @@ __device__ void mx_solve_t(const float* U, int ld, int n, float* D, const float*
       const float rdl = (lane < rn) ? rd[r0 + lane] : 0.0f;
       float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
 #pragma unroll
-      for (int t = 0; t < 32; ++t) {
-        if (t < rn) {
-          const float yt = __shfl_sync(0xffffffffu, v * rdl, t);
-          if (lane == t) v = yt;
-          else if (lane > t) v = fmaf(-col[t], yt, v);
-        }
+      for (int t = 0; t < 32; ++t) {  // lanes >= rn carry zeros, so all 32 steps run
+        const float yt = __shfl_sync(0xffffffffu, v * rdl, t);
+        v = (lane == t) ? yt : ((lane > t) ? fmaf(-col[t], yt, v) : v);
       }
       if (lane < rn) D[c * n + r0 + lane] = v;
     }
@@ -558,11 +551,8 @@ __device__ void mx_solve_t(const float* U, int ld, int n, float* D, const float*
       float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
 #pragma unroll
       for (int tt = 31; tt >= 0; --tt) {
-        if (tt < rn) {
-          const float xt = __shfl_sync(0xffffffffu, v * rdl, tt);
-          if (lane == tt) v = xt;
-          else if (lane < tt) v = fmaf(-row[tt], xt, v);
-        }
+        const float xt = __shfl_sync(0xffffffffu, v * rdl, tt);
+        v = (lane == tt) ? xt : ((lane < tt) ? fmaf(-row[tt], xt, v) : v);
       }
       if (lane < rn) D[c * n + r0 + lane] = v;
     }
@@ -623,7 +613,7 @@ __device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], flo
 // finishes vector c.  Per-warp maxima of |r| and the row sums of |A| (for
 // ||A||_inf) land in sm.red / sm.red2.
 template <int NC>
-__device__ void mx_residual_t(const double* __restrict__ A, int n, const double* __restrict__ B,
+__device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, const double* __restrict__ B,
                               const float* XH, const float* XL, float* D, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   float rmax = 0.0f;   // lane c: max |r| of vector c
@@ -695,7 +685,7 @@ __device__ void mx_residual_t(const double* __restrict__ A, int n, const double*
 // x += d in double-float (TwoSum then Fast2Sum renormalisation) for live
 // vectors; per-warp max |x| into sm.red2[warp][1 + c].
 template <int NC>
-__device__ void mx_update_x(int n, const float* D, float* XH, float* XL, MxSmem& sm) {
+__device__ __noinline__ void mx_update_x(int n, const float* D, float* XH, float* XL, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float xm[NC];
 #pragma unroll
