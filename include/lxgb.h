@@ -274,6 +274,23 @@ int lxgb_poisson5_f64(int64_t nx, int64_t ny, int32_t k, double scale,
                       const double* u, double* out, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Tensor-core GEMM.                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* C = alpha * A Bᵀ + beta * C on the tcgen05 tensor cores with TF32 inputs
+ * and FP32 accumulation in tensor memory.  A is m×k, B is n×k (row-major, k
+ * contiguous; lda, ldb multiples of 4, A and B 16-byte aligned), C is m×n
+ * row-major FP32.  *err (device int) is set to 1 if a pipeline wait timed out
+ * (the result is then incomplete); the caller zeroes it.  The trailing-matrix
+ * update of the mixed-precision LU (A22 -= L21 U12), the dense contraction of
+ * the blocked factorisations that lineax reaches through getrf
+ * (lineax/_solver/lu.py:53). */
+int lxgb_gemm_tf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
+                      int64_t lda, const float* b, int64_t ldb, float* c,
+                      int64_t ldc, float alpha, float beta, int32_t* err,
+                      void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */
 

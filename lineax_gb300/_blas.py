@@ -57,3 +57,26 @@ def any_nonfinite(x: torch.Tensor) -> torch.Tensor:
     _ffi.call("lxgb_nonfinite_f64", xf.numel(), _ffi.ptr(xf), _ffi.ptr(flag),
               _ffi.stream_handle(x.device))
     return flag
+
+
+def gemm_tf32_nt(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor | None = None,
+                 alpha: float = 1.0, beta: float = 0.0) -> torch.Tensor:
+    """alpha * a @ b.T + beta * c on the tcgen05 tensor cores (TF32 products,
+    FP32 accumulation).  a: (m, k), b: (n, k) float32 CUDA tensors with row
+    strides that are multiples of 4."""
+    if a.dtype != torch.float32 or b.dtype != torch.float32:
+        raise ValueError("gemm_tf32_nt takes float32 operands")
+    m, k = a.shape
+    n, k2 = b.shape
+    if k != k2:
+        raise ValueError("inner dimensions differ")
+    if c is None:
+        c = torch.zeros((m, n), dtype=torch.float32, device=a.device)
+        beta = 0.0
+    err = torch.zeros(1, dtype=torch.int32, device=a.device)
+    _ffi.call("lxgb_gemm_tf32_nt", m, n, k, _ffi.ptr(a), a.stride(0), _ffi.ptr(b), b.stride(0),
+              _ffi.ptr(c), c.stride(0), float(alpha), float(beta), _ffi.ptr(err),
+              _ffi.stream_handle(a.device))
+    if int(err.item()) != 0:
+        raise RuntimeError("tcgen05 GEMM pipeline timed out")
+    return c

@@ -78,6 +78,10 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "lxgb_kreduce_f64": (
         ctypes.c_int, [c_i32, c_i32, c_i64, c_p, c_i64, c_p, c_i64, c_p, c_p, c_i64, c_p]),
     "lxgb_poisson5_f64": (ctypes.c_int, [c_i64, c_i64, c_i32, c_f64, c_p, c_p, c_p]),
+    "lxgb_gemm_tf32_nt": (
+        ctypes.c_int,
+        [c_i32, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_i64, ctypes.c_float, ctypes.c_float,
+         c_p, c_p]),
     "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
     "lxgb_gemv_f64": (
         ctypes.c_int,

@@ -1,0 +1,321 @@
+// Tensor-core GEMM on the 5th-generation tensor cores (tcgen05), TF32 inputs,
+// FP32 accumulation in tensor memory:  C = alpha * A Bᵀ + beta * C.
+//
+// A is M×K and B is N×K, both row-major with K contiguous (K-major operands);
+// C is M×N row-major.  This is the trailing-matrix update of the blocked
+// factorisations (A22 -= L21 U12 with B = U12ᵀ).
+//
+// One CTA of 128 threads computes a 128×128 tile of C:
+//   * warp 0 / lane 0 streams 128×32 tiles of A and B into shared memory with
+//     TMA (cp.async.bulk.tensor, 128-byte swizzle) through a kStages-deep ring
+//     guarded by "full" / "empty" mbarriers;
+//   * warp 1 / lane 0 issues tcgen05.mma (M=128, N=128, K=8 per instruction)
+//     into a 128-column FP32 accumulator in tensor memory and returns each
+//     stage to the producer with tcgen05.commit;
+//   * all four warps read the accumulator back with tcgen05.ld (each warp owns
+//     32 TMEM lanes = 32 rows) and update C.
+// Every mbarrier wait is bounded: on timeout the kernel records an error code
+// in *err, waits (bounded) for the MMAs it issued, frees its tensor memory and
+// returns, so a broken pipeline cannot hang the GPU.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "common.cuh"
+
+namespace lxgb {
+
+constexpr int kTcM = 128;
+constexpr int kTcN = 128;
+constexpr int kTcK = 32;        // K elements per stage (128 bytes of FP32 = one swizzle row)
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 128;
+constexpr int kTcTileBytes = kTcM * kTcK * 4;  // 16 KB per operand tile
+constexpr unsigned kSpinLimit = 1u << 26;      // bounded mbarrier waits
+
+struct TcSmem {
+  alignas(1024) float a[kTcStages][kTcM * kTcK];
+  alignas(1024) float b[kTcStages][kTcN * kTcK];
+  alignas(8) unsigned long long full[kTcStages];
+  alignas(8) unsigned long long empty[kTcStages];
+  alignas(8) unsigned long long done;
+  unsigned tmem_base;
+  int abort;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Returns true when the phase with the given parity has completed, false on
+// timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  const unsigned addr = smem_u32(bar);
+  for (unsigned it = 0; it < kSpinLimit; ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row groups 1024 bytes apart (stride byte offset), descriptor
+// version 1 (bits 46-47), layout type 2 = SWIZZLE_128B (bits 61-63).
+__device__ __forceinline__ unsigned long long smem_desc_sw128(const void* p) {
+  const unsigned long long addr = (smem_u32(p) & 0x3FFFFu) >> 4;
+  const unsigned long long lbo = 1;            // unused by swizzled K-major layouts
+  const unsigned long long sbo = 1024 >> 4;
+  return addr | (lbo << 16) | (sbo << 32) | (1ull << 46) | (2ull << 61);
+}
+
+// Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
+// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+__host__ __device__ constexpr unsigned idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(n >> 3) << 17) |
+         ((unsigned)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(unsigned tmem_d, unsigned long long adesc,
+                                         unsigned long long bdesc, unsigned idesc, int accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
+  unsigned r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
+                    const __grid_constant__ CUtensorMap map_b, int M, int N, int K, float* C,
+                    int64_t ldc, float alpha, float beta, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  const int ktiles = (K + kTcK - 1) / kTcK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
+    }
+    mbar_init(&sm.done, 1);
+    sm.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // 128 TMEM columns for the 128×128 FP32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+                     smem_u32(&sm.tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = sm.tmem_base;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int t = 0; t < ktiles; ++t) {
+      const int s = t % kTcStages, r = t / kTcStages;
+      if (!mbar_wait(&sm.empty[s], (r & 1) ^ 1)) { atomicExch(&sm.abort, 1); break; }
+      if (*reinterpret_cast<volatile int*>(&sm.abort)) break;
+      mbar_expect_tx(&sm.full[s], 2 * kTcTileBytes);
+      tma_load_2d(sm.a[s], &map_a, t * kTcK, m0, &sm.full[s]);
+      tma_load_2d(sm.b[s], &map_b, t * kTcK, n0, &sm.full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr unsigned idesc = idesc_tf32(kTcM, kTcN);
+    int issued = 0;
+    for (int t = 0; t < ktiles; ++t) {
+      const int s = t % kTcStages, r = t / kTcStages;
+      if (!mbar_wait(&sm.full[s], r & 1)) { atomicExch(&sm.abort, 1); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int k = 0; k < kTcK / 8; ++k) {  // K = 8 TF32 (32 bytes) per instruction
+        const unsigned long long ad = smem_desc_sw128(sm.a[s]) + ((k * 32) >> 4);
+        const unsigned long long bd = smem_desc_sw128(sm.b[s]) + ((k * 32) >> 4);
+        mma_tf32(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+      }
+      mma_commit(&sm.empty[s]);
+      issued = 1;
+    }
+    if (issued) {
+      mma_commit(&sm.done);
+    } else {
+      // nothing issued (K == 0 or abort before the first stage): release the epilogue
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sm.done)) : "memory");
+    }
+  }
+  __syncwarp();
+  const bool done_ok = mbar_wait(&sm.done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!done_ok || sm.abort) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  } else {
+    // Epilogue: warp w owns rows 32w..32w+31 (TMEM lanes), 32 columns per load.
+    const int row = m0 + warp * 32 + lane;
+    const bool has_acc = ktiles > 0;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcN; c0 += 32) {
+      float v[32];
+      if (has_acc) {
+        tmem_ld32(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0, v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = 0.0f;
+      }
+      if (row < M) {
+        float* crow = C + (int64_t)row * ldc + n0 + c0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          if (n0 + c0 + i < N) {
+            const float old = (beta == 0.0f) ? 0.0f : beta * crow[i];
+            crow[i] = fmaf(alpha, v[i], old);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+  }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D FP32 map over rows×cols (row stride ld elements), box kTcK × 128.
+static int make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_last_error("gemm_tf32: cuTensorMapEncodeTiled unavailable");
+    return LXGB_CUDA_ERROR;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float))};
+  cuuint32_t box[2] = {(cuuint32_t)kTcK, 128u};
+  cuuint32_t estr[2] = {1u, 1u};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_last_error("gemm_tf32: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return LXGB_INVALID_ARG;
+  }
+  return LXGB_SUCCESSFUL;
+}
+
+__global__ void scale_c_kernel(int M, int N, float* C, int64_t ldc, float beta) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)M * N) return;
+  float* p = C + (e / N) * ldc + (e % N);
+  *p = (beta == 0.0f) ? 0.0f : beta * *p;
+}
+
+int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                 float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return LXGB_SUCCESSFUL;
+  if (K == 0) {  // C = beta * C
+    const int64_t total = (int64_t)M * N;
+    scale_c_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(M, N, C, ldc, beta);
+    return check_launch("gemm_tf32 (k = 0)");
+  }
+  CUtensorMap ma, mb;
+  int rc = make_map(&ma, A, M, K, lda);
+  if (rc) return rc;
+  rc = make_map(&mb, B, N, K, ldb);
+  if (rc) return rc;
+  const size_t smem = sizeof(TcSmem) + 1024;
+  LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                "gemm_tf32: set smem");
+  dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
+  gemm_tf32_nt_kernel<<<grid, kTcThreads, smem, st>>>(ma, mb, M, N, K, C, ldc, alpha, beta, err);
+  return check_launch("gemm_tf32");
+}
+
+}  // namespace lxgb
+
+using namespace lxgb;
+
+extern "C" int lxgb_gemm_tf32_nt(int32_t m, int32_t n, int32_t k, const float* a, int64_t lda,
+                                 const float* b, int64_t ldb, float* c, int64_t ldc, float alpha,
+                                 float beta, int32_t* err, void* stream) {
+  LXGB_REQUIRE(m >= 0 && n >= 0 && k >= 0, "gemm_tf32: negative size");
+  if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(c && err && (k == 0 || (a && b)), "gemm_tf32: null pointer");
+  LXGB_REQUIRE(ldc >= n, "gemm_tf32: ldc < n");
+  if (k > 0) {
+    LXGB_REQUIRE(lda >= k && ldb >= k, "gemm_tf32: leading dimension too small");
+    LXGB_REQUIRE((lda % 4) == 0 && (ldb % 4) == 0, "gemm_tf32: lda and ldb must be multiples of 4");
+    LXGB_REQUIRE((((uintptr_t)a) & 15) == 0 && (((uintptr_t)b) & 15) == 0,
+                 "gemm_tf32: A and B must be 16-byte aligned");
+  }
+  return gemm_tf32_nt(m, n, k, a, lda, b, ldb, c, ldc, alpha, beta, err, as_stream(stream));
+}

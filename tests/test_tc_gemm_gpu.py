@@ -1,0 +1,44 @@
+"""GPU: the tcgen05 TF32 GEMM (C = alpha A Bᵀ + beta C) against an FP32
+reference of the same operation."""
+
+import pytest
+import torch
+
+from lineax_gb300 import _blas
+
+pytestmark = pytest.mark.gpu
+
+
+def ref(a, b, c, alpha, beta):
+    torch.backends.cuda.matmul.allow_tf32 = False
+    out = alpha * (a.double() @ b.double().T)
+    if c is not None:
+        out = out + beta * c.double()
+    return out
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (128, 128, 8), (256, 384, 200), (1000, 700, 64),
+                                   (130, 260, 96), (512, 512, 512), (64, 128, 300)])
+def test_tf32_gemm_matches_fp32_reference(dev, m, n, k):
+    g = torch.Generator(device=dev).manual_seed(m * 131 + n * 7 + k)
+    a = torch.randn(m, k, device=dev, generator=g)
+    b = torch.randn(n, k, device=dev, generator=g)
+    c = torch.randn(m, n, device=dev, generator=g)
+    c0 = c.clone()
+    out = _blas.gemm_tf32_nt(a, b, c, alpha=-1.0, beta=1.0)
+    r = ref(a, b, c0, -1.0, 1.0)
+    # TF32 keeps 10 mantissa bits: per-product relative error <= 2^-10; the
+    # sum of k products is bounded by k * 2^-10 * max|a||b| (stated bound).
+    bound = (k * 2.0 ** -10) * float(a.abs().max() * b.abs().max()) + 1e-5
+    assert float((out.double() - r).abs().max()) <= bound
+    # and the typical error is that of TF32 rounding, far below the bound
+    rel = float((out.double() - r).norm() / r.norm())
+    assert rel < 5e-3, rel
+
+
+def test_tf32_gemm_beta_zero_and_k_zero(dev):
+    a = torch.randn(200, 0, device=dev)
+    b = torch.randn(150, 0, device=dev)
+    c = torch.full((200, 150), 3.0, device=dev)
+    _blas.gemm_tf32_nt(a, b, c, alpha=1.0, beta=0.5)
+    assert torch.allclose(c, torch.full_like(c, 1.5))
