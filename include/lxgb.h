@@ -290,6 +290,37 @@ int lxgb_gemm_tf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
                       int64_t ldc, float alpha, float beta, int32_t* err,
                       void* stream);
 
+/* The same with 3xTF32 products: a = a_hi + a_lo, b = b_hi + b_lo where the
+ * hi parts are TF32-exact (a and b pass the hi parts; a_lo, b_lo share their
+ * leading dimensions), C += alpha (Ah Bhᵀ + Ah Blᵀ + Al Bhᵀ): FP32-level
+ * accuracy from three tensor-core products per step. */
+int lxgb_gemm_3xtf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
+                        const float* a_lo, int64_t lda, const float* b,
+                        const float* b_lo, int64_t ldb, float* c, int64_t ldc,
+                        float alpha, float beta, int32_t* err, void* stream);
+
+/* Mixed-precision LU for GMRES-IR: P A = L U in FP32 with partial pivoting
+ * (first row of max |a|), 64-column panels, trailing updates on the tcgen05
+ * tensor cores with FP32 accumulation: precision 0 = TF32 products, 1 =
+ * 3xTF32 (hi/lo operand split, FP32-level accuracy).  If a64 is not NULL the
+ * row-major FP64 matrix is first rounded into lu (n×n FP32, 16-byte aligned);
+ * otherwise lu already holds the FP32 matrix.  n must be a multiple of 4.
+ * piv: 0-based swaps; info as getrf; *err (device, zeroed by the caller) = 1
+ * if a tensor-core pipeline wait timed out.  `work`: 256-byte aligned,
+ * lxgb_getrf_f32_tc_workspace_size(n) bytes.  The low-precision factor of
+ * the GMRES-IR configuration (lineax/_solver/gmres.py preconditioned by an LU
+ * of lineax/_solver/lu.py:53). */
+int64_t lxgb_getrf_f32_tc_workspace_size(int32_t n, int32_t precision);
+int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_t* piv,
+                      int32_t* info, int32_t precision, int32_t* err,
+                      void* work, int64_t work_bytes, void* stream);
+
+/* x_r = U^{-1} L^{-1} P b_r for nrhs FP64 vectors (length n, back to back),
+ * computed in FP32 with a factor from lxgb_getrf_f32_tc: the preconditioner
+ * apply of GMRES-IR.  b and x may not alias. */
+int lxgb_getrs_f32(int32_t n, int32_t nrhs, const float* lu, const int32_t* piv,
+                   const double* b, double* x, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */
@@ -332,6 +363,21 @@ int lxgb_nonfinite_f64(int64_t n, const double* x, int32_t* flag, void* stream);
 int64_t lxgb_reduce_workspace_size(int64_t n);
 int lxgb_reduce_f64(int32_t op, int64_t n, const double* x, const double* y,
                     double* out, void* work, int64_t work_bytes, void* stream);
+
+/* Blocks of k FP64 vectors of length n (vector c at x + c*n), per-vector
+ * scalars s[c] on the device:  x_c *= s[c] (invert: x_c *= 1/s[c], a zero
+ * scale giving zeros), and y_c += s[c] x_c.  The vector updates of the
+ * GMRES-IR outer loop (correction scaling, x += d). */
+int lxgb_rows_scale_f64(int32_t k, int64_t n, const double* s, int32_t invert,
+                        double* x, void* stream);
+int lxgb_rows_axpy_f64(int32_t k, int64_t n, const double* s, const double* x,
+                       double* y, void* stream);
+
+/* out[0] = ||A||_inf = max_i sum_j |a_ij| (device), for normwise backward
+ * errors; `work` holds lxgb_norm_inf_workspace_size(m) bytes. */
+int64_t lxgb_norm_inf_workspace_size(int64_t m);
+int lxgb_norm_inf_f64(int64_t m, int64_t n, const double* a, int64_t lda,
+                      double* out, void* work, int64_t work_bytes, void* stream);
 
 /* x_i = b_i / a[i*stride] (stride n+1 walks a matrix diagonal); with
  * well_posed == 0 a zero diagonal entry gives x_i = 0 (pseudo-inverse).

@@ -80,3 +80,26 @@ def gemm_tf32_nt(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor | None = None
     if int(err.item()) != 0:
         raise RuntimeError("tcgen05 GEMM pipeline timed out")
     return c
+
+
+def gemm_3xtf32_nt(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor | None = None,
+                   alpha: float = 1.0, beta: float = 0.0) -> torch.Tensor:
+    """alpha * a @ b.T + beta * c with 3xTF32 tensor-core products (FP32-level
+    accuracy): the operands are split into TF32-exact hi parts and lo remainders."""
+    def split(x):
+        hi = (x.view(torch.int32) & -8192).view(torch.float32).contiguous()
+        return hi, (x - hi).contiguous()
+    m, k = a.shape
+    n = b.shape[0]
+    ah, al = split(a.contiguous())
+    bh, bl = split(b.contiguous())
+    if c is None:
+        c = torch.zeros((m, n), dtype=torch.float32, device=a.device)
+        beta = 0.0
+    err = torch.zeros(1, dtype=torch.int32, device=a.device)
+    _ffi.call("lxgb_gemm_3xtf32_nt", m, n, k, _ffi.ptr(ah), _ffi.ptr(al), k, _ffi.ptr(bh),
+              _ffi.ptr(bl), k, _ffi.ptr(c), c.stride(0), float(alpha), float(beta), _ffi.ptr(err),
+              _ffi.stream_handle(a.device))
+    if int(err.item()) != 0:
+        raise RuntimeError("tcgen05 GEMM pipeline timed out")
+    return c

@@ -82,6 +82,13 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         ctypes.c_int,
         [c_i32, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_i64, ctypes.c_float, ctypes.c_float,
          c_p, c_p]),
+    "lxgb_getrf_f32_tc_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_getrf_f32_tc": (ctypes.c_int, [c_i32, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64, c_p]),
+    "lxgb_gemm_3xtf32_nt": (
+        ctypes.c_int,
+        [c_i32, c_i32, c_i32, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, ctypes.c_float,
+         ctypes.c_float, c_p, c_p]),
+    "lxgb_getrs_f32": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_p, c_p, c_p]),
     "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
     "lxgb_gemv_f64": (
         ctypes.c_int,
@@ -90,6 +97,10 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "lxgb_nonfinite_f64": (ctypes.c_int, [c_i64, c_p, c_p, c_p]),
     "lxgb_reduce_workspace_size": (c_i64, [c_i64]),
     "lxgb_reduce_f64": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_rows_scale_f64": (ctypes.c_int, [c_i32, c_i64, c_p, c_i32, c_p, c_p]),
+    "lxgb_rows_axpy_f64": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p]),
+    "lxgb_norm_inf_workspace_size": (c_i64, [c_i64]),
+    "lxgb_norm_inf_f64": (ctypes.c_int, [c_i64, c_i64, c_p, c_i64, c_p, c_p, c_i64, c_p]),
     "lxgb_diag_solve_f64": (ctypes.c_int, [c_i64, c_p, c_i64, c_p, c_p, c_i32, c_p]),
 }
 

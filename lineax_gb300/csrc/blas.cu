@@ -135,9 +135,92 @@ static int reduce_parts(int64_t n) {
   return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
+// Row-wise helpers for blocks of k vectors of length n (vector c at x + c*n):
+// scale x_c by s[c] (or 1/s[c]; a zero scale leaves zeros), and y_c += s[c] x_c.
+__global__ void rows_scale_kernel(int k, int64_t n, const double* __restrict__ s, int invert,
+                                  double* __restrict__ x) {
+  const int c = blockIdx.y;
+  const double sc = s[c];
+  const double f = invert ? (sc != 0.0 ? 1.0 / sc : 0.0) : sc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[(int64_t)c * n + i] *= f;
+}
+
+__global__ void rows_axpy_kernel(int k, int64_t n, const double* __restrict__ s,
+                                 const double* __restrict__ x, double* __restrict__ y) {
+  const int c = blockIdx.y;
+  const double sc = s[c];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[(int64_t)c * n + i] = fma(sc, x[(int64_t)c * n + i], y[(int64_t)c * n + i]);
+}
+
+// out = max_i sum_j |a_ij| (||A||_inf), one warp per row, fixed combination order.
+__global__ void __launch_bounds__(256)
+norm_inf_partial_kernel(int64_t m, int64_t n, const double* __restrict__ a, int64_t lda,
+                        double* __restrict__ part) {
+  __shared__ double sm[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double best = 0.0;
+  for (int64_t i = blockIdx.x * 8LL + warp; i < m; i += (int64_t)gridDim.x * 8) {
+    double acc = 0.0;
+    for (int64_t j = lane; j < n; j += 32) acc += fabs(a[i * lda + j]);
+    acc = warp_sum(acc);
+    best = nanmax(best, acc);
+  }
+  if (lane == 0) sm[warp] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = sm[0];
+    for (int w = 1; w < 8; ++w) t = nanmax(t, sm[w]);
+    part[blockIdx.x] = t;
+  }
+}
+
 }  // namespace lxgb
 
 using namespace lxgb;
+
+extern "C" int lxgb_rows_scale_f64(int32_t k, int64_t n, const double* s, int32_t invert,
+                                   double* x, void* stream) {
+  LXGB_REQUIRE(k >= 0 && k <= 65535 && n >= 0, "rows_scale: bad sizes");
+  if (k == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(s && x, "rows_scale: null pointer");
+  const int64_t bx = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  rows_scale_kernel<<<dim3((unsigned)bx, (unsigned)k), 256, 0, as_stream(stream)>>>(k, n, s, invert, x);
+  return check_launch("rows_scale");
+}
+
+extern "C" int lxgb_rows_axpy_f64(int32_t k, int64_t n, const double* s, const double* x, double* y,
+                                  void* stream) {
+  LXGB_REQUIRE(k >= 0 && k <= 65535 && n >= 0, "rows_axpy: bad sizes");
+  if (k == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(s && x && y, "rows_axpy: null pointer");
+  const int64_t bx = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  rows_axpy_kernel<<<dim3((unsigned)bx, (unsigned)k), 256, 0, as_stream(stream)>>>(k, n, s, x, y);
+  return check_launch("rows_axpy");
+}
+
+extern "C" int lxgb_norm_inf_f64(int64_t m, int64_t n, const double* a, int64_t lda, double* out,
+                                 void* work, int64_t work_bytes, void* stream) {
+  LXGB_REQUIRE(m >= 0 && n >= 0 && out && work, "norm_inf: bad arguments");
+  LXGB_REQUIRE(m == 0 || (a && lda >= n), "norm_inf: bad matrix");
+  const int parts = reduce_parts(m * 32);
+  if (work_bytes < (int64_t)parts * 8) {
+    set_last_error("norm_inf: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  double* part = reinterpret_cast<double*>(work);
+  norm_inf_partial_kernel<<<parts, 256, 0, st>>>(m, n, a, lda, part);
+  reduce_final_kernel<<<1, 32, 0, st>>>(1, parts, 0, nullptr, part, out);
+  return check_launch("norm_inf");
+}
+
+extern "C" int64_t lxgb_norm_inf_workspace_size(int64_t m) {
+  return (int64_t)reduce_parts((m > 0 ? m : 1) * 32) * 8;
+}
 
 extern "C" int64_t lxgb_reduce_workspace_size(int64_t n) {
   return (int64_t)reduce_parts(n < 0 ? 0 : n) * (int64_t)sizeof(double);

@@ -27,16 +27,20 @@ namespace lxgb {
 constexpr int kTcM = 128;
 constexpr int kTcN = 128;
 constexpr int kTcK = 32;        // K elements per stage (128 bytes of FP32 = one swizzle row)
-constexpr int kTcStages = 4;
+constexpr int kTcStages = 4;       // TF32: 32 KB per stage
+constexpr int kTcStagesSplit = 3;  // 3xTF32: 64 KB per stage (hi and lo tiles)
 constexpr int kTcThreads = 128;
 constexpr int kTcTileBytes = kTcM * kTcK * 4;  // 16 KB per operand tile
 constexpr unsigned kSpinLimit = 1u << 26;      // bounded mbarrier waits
 
+template <int S, bool SPLIT>
 struct TcSmem {
-  alignas(1024) float a[kTcStages][kTcM * kTcK];
-  alignas(1024) float b[kTcStages][kTcN * kTcK];
-  alignas(8) unsigned long long full[kTcStages];
-  alignas(8) unsigned long long empty[kTcStages];
+  alignas(1024) float a[S][kTcM * kTcK];
+  alignas(1024) float b[S][kTcN * kTcK];
+  alignas(1024) float al[SPLIT ? S : 1][SPLIT ? kTcM * kTcK : 1];
+  alignas(1024) float bl[SPLIT ? S : 1][SPLIT ? kTcN * kTcK : 1];
+  alignas(8) unsigned long long full[S];
+  alignas(8) unsigned long long empty[S];
   alignas(8) unsigned long long done;
   unsigned tmem_base;
   int abort;
@@ -134,19 +138,27 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// SPLIT (3xTF32): A = Ah + Al and B = Bh + Bl with TF32-exact hi parts;
+// A Bᵀ ~= Ah Bhᵀ + Ah Blᵀ + Al Bhᵀ accumulated in the same tensor memory,
+// which restores FP32-level accuracy.
+template <bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 1)
 gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
-                    const __grid_constant__ CUtensorMap map_b, int M, int N, int K, float* C,
+                    const __grid_constant__ CUtensorMap map_b,
+                    const __grid_constant__ CUtensorMap map_al,
+                    const __grid_constant__ CUtensorMap map_bl, int M, int N, int K, float* C,
                     int64_t ldc, float alpha, float beta, int* err) {
+  constexpr int kStages = SPLIT ? kTcStagesSplit : kTcStages;
+  using Smem = TcSmem<kStages, SPLIT>;
   extern __shared__ unsigned char smem_raw[];
-  TcSmem& sm = *reinterpret_cast<TcSmem*>(
+  Smem& sm = *reinterpret_cast<Smem*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
   const int ktiles = (K + kTcK - 1) / kTcK;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kTcStages; ++s) {
+    for (int s = 0; s < kStages; ++s) {
       mbar_init(&sm.full[s], 1);
       mbar_init(&sm.empty[s], 1);
     }
@@ -168,19 +180,23 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
   if (warp == 0 && lane == 0) {
     // TMA producer
     for (int t = 0; t < ktiles; ++t) {
-      const int s = t % kTcStages, r = t / kTcStages;
+      const int s = t % kStages, r = t / kStages;
       if (!mbar_wait(&sm.empty[s], (r & 1) ^ 1)) { atomicExch(&sm.abort, 1); break; }
       if (*reinterpret_cast<volatile int*>(&sm.abort)) break;
-      mbar_expect_tx(&sm.full[s], 2 * kTcTileBytes);
+      mbar_expect_tx(&sm.full[s], (SPLIT ? 4 : 2) * kTcTileBytes);
       tma_load_2d(sm.a[s], &map_a, t * kTcK, m0, &sm.full[s]);
       tma_load_2d(sm.b[s], &map_b, t * kTcK, n0, &sm.full[s]);
+      if constexpr (SPLIT) {
+        tma_load_2d(sm.al[s], &map_al, t * kTcK, m0, &sm.full[s]);
+        tma_load_2d(sm.bl[s], &map_bl, t * kTcK, n0, &sm.full[s]);
+      }
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     constexpr unsigned idesc = idesc_tf32(kTcM, kTcN);
     int issued = 0;
     for (int t = 0; t < ktiles; ++t) {
-      const int s = t % kTcStages, r = t / kTcStages;
+      const int s = t % kStages, r = t / kStages;
       if (!mbar_wait(&sm.full[s], r & 1)) { atomicExch(&sm.abort, 1); break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
@@ -188,6 +204,12 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
         const unsigned long long ad = smem_desc_sw128(sm.a[s]) + ((k * 32) >> 4);
         const unsigned long long bd = smem_desc_sw128(sm.b[s]) + ((k * 32) >> 4);
         mma_tf32(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+        if constexpr (SPLIT) {
+          const unsigned long long ald = smem_desc_sw128(sm.al[s]) + ((k * 32) >> 4);
+          const unsigned long long bld = smem_desc_sw128(sm.bl[s]) + ((k * 32) >> 4);
+          mma_tf32(tmem, ad, bld, idesc, 1);
+          mma_tf32(tmem, ald, bd, idesc, 1);
+        }
       }
       mma_commit(&sm.empty[s]);
       issued = 1;
@@ -278,35 +300,99 @@ __global__ void scale_c_kernel(int M, int N, float* C, int64_t ldc, float beta) 
   *p = (beta == 0.0f) ? 0.0f : beta * *p;
 }
 
-int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb,
-                 float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
+int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int64_t lda,
+                       const float* B, const float* Bl, int64_t ldb, float* C, int64_t ldc,
+                       float alpha, float beta, int* err, cudaStream_t st) {
   if (M <= 0 || N <= 0) return LXGB_SUCCESSFUL;
   if (K == 0) {  // C = beta * C
     const int64_t total = (int64_t)M * N;
     scale_c_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(M, N, C, ldc, beta);
     return check_launch("gemm_tf32 (k = 0)");
   }
-  CUtensorMap ma, mb;
+  const bool split = (Al != nullptr) && (Bl != nullptr);
+  CUtensorMap ma, mb, mal, mbl;
   int rc = make_map(&ma, A, M, K, lda);
   if (rc) return rc;
   rc = make_map(&mb, B, N, K, ldb);
   if (rc) return rc;
-  const size_t smem = sizeof(TcSmem) + 1024;
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                "gemm_tf32: set smem");
+  mal = ma;
+  mbl = mb;
+  if (split) {
+    rc = make_map(&mal, Al, M, K, lda);
+    if (rc) return rc;
+    rc = make_map(&mbl, Bl, N, K, ldb);
+    if (rc) return rc;
+  }
   dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
-  gemm_tf32_nt_kernel<<<grid, kTcThreads, smem, st>>>(ma, mb, M, N, K, C, ldc, alpha, beta, err);
+  if (split) {
+    const size_t smem = sizeof(TcSmem<kTcStagesSplit, true>) + 1024;
+    LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                  "gemm_tf32: set smem");
+    gemm_tf32_nt_kernel<true><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, M, N, K, C, ldc,
+                                                             alpha, beta, err);
+  } else {
+    const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
+    LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                  "gemm_tf32: set smem");
+    gemm_tf32_nt_kernel<false><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, M, N, K, C, ldc,
+                                                              alpha, beta, err);
+  }
   return check_launch("gemm_tf32");
+}
+
+int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb,
+                 float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
+  return gemm_tf32_nt_split(M, N, K, A, nullptr, lda, B, nullptr, ldb, C, ldc, alpha, beta, err,
+                            st);
+}
+
+// hi = x with the low 13 mantissa bits cleared (TF32-exact), lo = x - hi
+// (exact in FP32): the operand split of 3xTF32.
+__global__ void tf32_split_kernel(int64_t rows, int64_t cols, const float* __restrict__ src,
+                                  int64_t lds, float* __restrict__ hi, float* __restrict__ lo,
+                                  int64_t ldd) {
+  const int64_t total = rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / cols, c = e % cols;
+    const float x = src[r * lds + c];
+    const float h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    hi[r * ldd + c] = h;
+    lo[r * ldd + c] = x - h;
+  }
+}
+
+int tf32_split(int64_t rows, int64_t cols, const float* src, int64_t lds, float* hi, float* lo,
+               int64_t ldd, cudaStream_t st) {
+  const int64_t total = rows * cols;
+  if (total <= 0) return LXGB_SUCCESSFUL;
+  const int64_t blocks = (total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096;
+  tf32_split_kernel<<<(unsigned)blocks, 256, 0, st>>>(rows, cols, src, lds, hi, lo, ldd);
+  return check_launch("tf32_split");
 }
 
 }  // namespace lxgb
 
 using namespace lxgb;
 
+extern "C" int lxgb_gemm_3xtf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
+                                   const float* a_lo, int64_t lda, const float* b,
+                                   const float* b_lo, int64_t ldb, float* c, int64_t ldc,
+                                   float alpha, float beta, int32_t* err, void* stream);
+
 extern "C" int lxgb_gemm_tf32_nt(int32_t m, int32_t n, int32_t k, const float* a, int64_t lda,
                                  const float* b, int64_t ldb, float* c, int64_t ldc, float alpha,
                                  float beta, int32_t* err, void* stream) {
+  return lxgb_gemm_3xtf32_nt(m, n, k, a, nullptr, lda, b, nullptr, ldb, c, ldc, alpha, beta, err,
+                             stream);
+}
+
+extern "C" int lxgb_gemm_3xtf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
+                                   const float* a_lo, int64_t lda, const float* b,
+                                   const float* b_lo, int64_t ldb, float* c, int64_t ldc,
+                                   float alpha, float beta, int32_t* err, void* stream) {
   LXGB_REQUIRE(m >= 0 && n >= 0 && k >= 0, "gemm_tf32: negative size");
   if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
   LXGB_REQUIRE(c && err && (k == 0 || (a && b)), "gemm_tf32: null pointer");
@@ -317,5 +403,9 @@ extern "C" int lxgb_gemm_tf32_nt(int32_t m, int32_t n, int32_t k, const float* a
     LXGB_REQUIRE((((uintptr_t)a) & 15) == 0 && (((uintptr_t)b) & 15) == 0,
                  "gemm_tf32: A and B must be 16-byte aligned");
   }
-  return gemm_tf32_nt(m, n, k, a, lda, b, ldb, c, ldc, alpha, beta, err, as_stream(stream));
+  LXGB_REQUIRE((a_lo == nullptr) == (b_lo == nullptr), "gemm_3xtf32: give both lo parts or none");
+  LXGB_REQUIRE((((uintptr_t)a_lo) & 15) == 0 && (((uintptr_t)b_lo) & 15) == 0,
+               "gemm_3xtf32: lo parts must be 16-byte aligned");
+  return gemm_tf32_nt_split(m, n, k, a, a_lo, lda, b, b_lo, ldb, c, ldc, alpha, beta, err,
+                            as_stream(stream));
 }
