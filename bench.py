@@ -395,6 +395,105 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Secondary workload: mixed-precision LU + GMRES-IR (dense n×n, 16 RHS)
+# ---------------------------------------------------------------------------
+def haar_conditioned(n, cond, seed, dev):
+    """A = U diag(sigma) Vᵀ, U and V Haar-orthogonal (QR of a Gaussian with the
+    sign fix), sigma log-spaced from 1 to 1/cond.  Generated on the GPU with
+    torch (input preparation, not part of any timed region)."""
+    import torch
+
+    g = torch.Generator(device=dev).manual_seed(seed)
+
+    def haar():
+        q, r = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=dev, generator=g))
+        return q * torch.sign(torch.diagonal(r))
+
+    u, v = haar(), haar()
+    sig = torch.logspace(0, -float(__import__("math").log10(cond)), n, dtype=torch.float64,
+                         device=dev)
+    a = (u * sig) @ v.T
+    del u, v
+    return a.contiguous()
+
+
+def run_gmres_ir(args):
+    """Dense n×n, 16 right-hand sides, cond in {1e2, 1e6, 1e10}: FP32 LU with
+    TF32 or 3xTF32 tensor-core updates + GMRES-IR to backward error <= 1e-12,
+    against the plain FP64 LU of this library.  One JSON line per case."""
+    import time
+
+    import torch
+
+    from lineax_gb300 import _dense, mixed
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    n, k = args.n, 16
+    g = torch.Generator(device=dev).manual_seed(11)
+    b = torch.randn(k, n, dtype=torch.float64, device=dev, generator=g)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def emit(obj):
+        obj.update({"workload": f"gmres_ir_dense_n{n}_16rhs", "n": n, "nrhs": k})
+        print(json.dumps(obj), flush=True)
+
+    # warm-up: module load and first-call costs of every kernel used below
+    a0 = haar_conditioned(256, 1e2, 1, dev)
+    for prec in ("tf32", "3xtf32"):
+        mixed.gmres_ir(a0, b[:, :256].contiguous(), precision=prec, restart=args.restart)
+    lu0, piv0 = _dense.lu_factor(a0)
+    _dense.lu_solve(lu0, piv0, b[:, :256].contiguous())
+    torch.cuda.synchronize()
+    for cond in (1e2, 1e6, 1e10):
+        a = haar_conditioned(n, cond, 5, dev)
+        anorm = float(mixed.norm_inf(a).item())
+        bn = b.abs().amax(dim=1)
+        if cond == 1e2 or args.fp64_all:
+            e0, e1, e2 = ev(), ev(), ev()
+            e0.record()
+            lu, piv = _dense.lu_factor(a)
+            e1.record()
+            x = _dense.lu_solve(lu, piv, b)
+            e2.record()
+            torch.cuda.synchronize()
+            r = b - (a @ x.T).T
+            berr = (r.abs().amax(dim=1) / (anorm * x.abs().amax(dim=1) + bn)).max().item()
+            emit({"case": "fp64_lu", "cond": cond, "factor_ms": e0.elapsed_time(e1),
+                  "solve_ms": e1.elapsed_time(e2), "total_ms": e0.elapsed_time(e2),
+                  "max_berr": berr, "solves_per_s": k / (e0.elapsed_time(e2) * 1e-3)})
+            del lu, x
+            torch.cuda.empty_cache()
+        for prec in ("tf32", "3xtf32"):
+            t0 = time.perf_counter()
+            e = [ev() for _ in range(5)]
+            e[0].record()
+            f = mixed.lu_factor_tf32(a, prec)
+            e[1].record()
+            inv = mixed.lu_inverse(f, prec)
+            e[2].record()
+            sp = mixed.split_matrix(a)
+            e[3].record()
+            res = mixed.gmres_ir(a, b, tol=1e-12, restart=args.restart, max_outer=10,
+                                 inner_max_steps=args.inner_max_steps, factor=f, inverse=inv,
+                                 split=sp, precision=prec, arith="df", fallback=True)
+            e[4].record()
+            torch.cuda.synchronize()
+            total = e[0].elapsed_time(e[4])
+            emit({"case": f"gmres_ir_{prec}", "cond": cond, "restart": args.restart,
+                  "factor_ms": e[0].elapsed_time(e[1]), "inverse_ms": e[1].elapsed_time(e[2]),
+                  "split_ms": e[2].elapsed_time(e[3]), "refine_ms": e[3].elapsed_time(e[4]),
+                  "total_ms": total, "outer": res.outer, "inner_cycles": res.inner_steps,
+                  "max_berr": max(res.berr), "converged": res.converged,
+                  "fp64_fallback": res.fallback,
+                  "solves_per_s": k / (total * 1e-3), "wall_s": time.perf_counter() - t0})
+            del f, inv, sp, res
+            torch.cuda.empty_cache()
+        del a
+        torch.cuda.empty_cache()
+
+
 def main():
     global COUNT
     p = argparse.ArgumentParser()
@@ -405,8 +504,20 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline measurement")
     p.add_argument("--systems", type=int, default=COUNT,
                    help="systems per GPU (smaller values are for profiling runs only)")
+    p.add_argument("--workload", default="ragged_cholesky",
+                   choices=["ragged_cholesky", "gmres_ir"],
+                   help="gmres_ir: the dense mixed-precision LU + GMRES-IR workload")
+    p.add_argument("--n", type=int, default=8192, help="order for --workload gmres_ir")
+    p.add_argument("--restart", type=int, default=20, help="GMRES restart for --workload gmres_ir")
+    p.add_argument("--inner-max-steps", type=int, default=20,
+                   help="GMRES restart cycles per refinement step before falling back to FP64")
+    p.add_argument("--fp64-all", action="store_true",
+                   help="time the plain FP64 LU at every condition number (gmres_ir)")
     args = p.parse_args()
     COUNT = args.systems
+    if args.workload == "gmres_ir":
+        run_gmres_ir(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

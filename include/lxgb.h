@@ -321,6 +321,46 @@ int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_t* piv,
 int lxgb_getrs_f32(int32_t n, int32_t nrhs, const float* lu, const int32_t* piv,
                    const double* b, double* x, void* stream);
 
+/* Inverse factors of a factor from lxgb_getrf_f32_tc: linv = L^{-1} (unit
+ * lower, zeros above the diagonal) and uinv = U^{-1} (zeros below), both
+ * row-major n×n FP32, and perm with (P b)_i = b[perm[i]].  Off-diagonal
+ * updates on the tensor cores: precision 0 TF32, 1 3xTF32.  n <= 25600,
+ * n % 4 == 0, lu 16-byte and work 256-byte aligned, work_bytes >=
+ * lxgb_lu32_inverse_workspace_size.  *err is set if a tensor-core pipeline
+ * wait gave up.  No reference counterpart: the build's GMRES-IR applies the
+ * preconditioner (lineax/_solver/gmres.py:106-240 with an LU of
+ * lineax/_solver/lu.py:53) as two triangular products with these. */
+int64_t lxgb_lu32_inverse_workspace_size(int32_t n, int32_t precision);
+int lxgb_lu32_inverse(int32_t n, const float* lu, const int32_t* piv,
+                      float* linv, float* uinv, int32_t* perm, int32_t precision,
+                      int32_t* err, void* work, int64_t work_bytes, void* stream);
+
+/* y_r = U^{-1} L^{-1} P x_r for nrhs FP64 vectors (length n, back to back)
+ * with the inverse factors above; mode 0 FP32 arithmetic, mode 1
+ * double-float (about 48 significant bits, FP64-accurate).  x and y may not
+ * alias. */
+int64_t lxgb_lu32_apply_workspace_size(int32_t n, int32_t nrhs);
+int lxgb_lu32_apply(int32_t n, int32_t nrhs, const float* linv,
+                    const float* uinv, const int32_t* perm, int32_t mode,
+                    const double* x, double* y, void* work, int64_t work_bytes,
+                    void* stream);
+
+/* hi = a truncated to 24 significant bits, lo = the next 24 (lo may be
+ * null): a row-major rows×cols FP64 block as an FP32 pair. */
+int lxgb_split_f64(int64_t rows, int64_t cols, const double* a, int64_t lda,
+                   float* hi, float* lo, int64_t ld, void* stream);
+
+/* y_r = A x_r, or y_r = b_r - A x_r when b is given (b_r at b + r*ldy), for
+ * nrhs vectors, A m×n given as FP32 hi (+ optional lo) with row stride lda.
+ * mode 0: FP32 arithmetic on hi; mode 1: double-float arithmetic (FP64
+ * accurate for hi + lo).  The operator product and residual of GMRES-IR
+ * (lineax/_operator.py:269 at FP64 accuracy). */
+int64_t lxgb_gemv_df_workspace_size(int32_t n, int32_t nrhs);
+int lxgb_gemv_df(int32_t m, int32_t n, const float* a_hi, const float* a_lo,
+                 int64_t lda, int32_t nrhs, const double* x, int64_t ldx,
+                 const double* b, double* y, int64_t ldy, int32_t mode,
+                 void* work, int64_t work_bytes, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */

@@ -89,6 +89,16 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i32, c_i32, c_i32, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, ctypes.c_float,
          ctypes.c_float, c_p, c_p]),
     "lxgb_getrs_f32": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_lu32_inverse_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_lu32_inverse": (ctypes.c_int, [c_i32, c_p, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64,
+                                         c_p]),
+    "lxgb_lu32_apply_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_lu32_apply": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_p, c_i32, c_p, c_p, c_p, c_i64,
+                                       c_p]),
+    "lxgb_split_f64": (ctypes.c_int, [c_i64, c_i64, c_p, c_i64, c_p, c_p, c_i64, c_p]),
+    "lxgb_gemv_df_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_gemv_df": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_i64, c_i32, c_p, c_i64, c_p, c_p,
+                                    c_i64, c_i32, c_p, c_i64, c_p]),
     "lxgb_trsm_f64": (ctypes.c_int, [c_i32, c_i32, c_p, c_i64, c_i32, c_i32, c_i32, c_p, c_p]),
     "lxgb_gemv_f64": (
         ctypes.c_int,

@@ -3,11 +3,17 @@
 // FP32 solve used as the preconditioner of FP64 GMRES-IR.
 //
 // Right-looking blocked LU with 64-column panels:
-//   panel_getf2_f32_kernel — getf2 on the panel (one CTA; first row of max |a|)
+//   panel_getf2_cluster_kernel — getf2 on the panel held in the shared memory
+//                            of a thread-block cluster (up to 16 CTAs); the
+//                            pivot search is exchanged through distributed
+//                            shared memory.  panel_getf2_f32_kernel (one
+//                            CTA, panel in global memory) covers panels too
+//                            tall for the cluster.
 //   laswp_f32_kernel       — the panel's row interchanges on the other columns
-//   trsm_blockrow_f32_kernel — U12 = L11^{-1} A12
-//   transpose_f32_kernel   — U12ᵀ into a K-major buffer for the GEMM
+//   launch_inv_diag_lower  — U12 = L11^{-1} A12 in place, and U12ᵀ into a
+//                            K-major buffer for the GEMM (ir.cu)
 //   gemm_tf32_nt           — A22 -= L21 U12 on the tensor cores
+#include <cooperative_groups.h>
 #include <float.h>
 #include <limits.h>
 
@@ -96,6 +102,166 @@ panel_getf2_f32_kernel(int n, int j0, int nb, float* __restrict__ a, int32_t* __
   }
 }
 
+namespace cg = cooperative_groups;
+
+constexpr int kPanelCluThreads = 512;
+constexpr int kPanelLd = kLu32NB + 1;  // padded row: column reads are conflict-free
+constexpr int kPanelCluMax = 16;
+constexpr size_t kPanelCluSmemMax = 200 * 1024;
+
+// getf2 on the m×nb panel at (j0, j0) (m = n - j0), rows split over the
+// cluster's CTAs (rows_per_cta each) and kept in shared memory for the whole
+// panel.  Per column: each CTA's first max |a| is published; after a cluster
+// barrier every CTA reduces the candidates (same order everywhere: first row
+// of max |a|, as isamax), copies the pivot row and row kk out of their owners'
+// shared memory, and after a second barrier the owners swap them and every CTA
+// scales and updates its own rows.  Candidates are double-buffered by column
+// parity, so one barrier pair per column suffices.  Arithmetic matches
+// panel_getf2_f32_kernel (reciprocal scaling, fmaf rank-1 updates).
+__global__ void __launch_bounds__(kPanelCluThreads)
+panel_getf2_cluster_kernel(int n, int j0, int nb, int rows_per_cta, float* __restrict__ a,
+                           int32_t* __restrict__ piv, int32_t* __restrict__ info) {
+  extern __shared__ float P[];
+  __shared__ float cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ float rowp[kLu32NB], rowk[kLu32NB];
+  __shared__ float s_wv[kPanelCluThreads / 32];
+  __shared__ int s_wi[kPanelCluThreads / 32];
+  __shared__ int s_p;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ncta = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int m = n - j0;
+  const int R = rows_per_cta;
+  const int r0 = rank * R;
+  const int mloc = max(0, min(R, m - r0));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (int e = tid; e < mloc * kLu32NB; e += blockDim.x) {
+    const int i = e / kLu32NB, j = e % kLu32NB;
+    P[i * kPanelLd + j] = (j < nb) ? a[(int64_t)(j0 + r0 + i) * n + j0 + j] : 0.0f;
+  }
+  __syncthreads();
+  for (int kk = 0; kk < nb; ++kk) {
+    const int par = kk & 1;
+    float v = -1.0f;
+    int idx = INT_MAX;
+    for (int i = tid; i < mloc; i += blockDim.x) {
+      if (r0 + i >= kk) {
+        const float x = fabsf(P[i * kPanelLd + kk]);
+        if (x > v) { v = x; idx = r0 + i; }
+      }
+    }
+    warp_argmax_first_f(v, idx);
+    if (lane == 0) { s_wv[warp] = v; s_wi[warp] = idx; }
+    __syncthreads();
+    if (warp == 0) {
+      v = lane < nwarps ? s_wv[lane] : -1.0f;
+      idx = lane < nwarps ? s_wi[lane] : INT_MAX;
+      warp_argmax_first_f(v, idx);
+      if (lane == 0) { cand_v[par] = v; cand_i[par] = idx; }
+    }
+    cluster.sync();
+    if (warp == 0) {
+      float cv = -1.0f;
+      int ci = INT_MAX;
+      if (lane < ncta) {
+        cv = *cluster.map_shared_rank(&cand_v[par], lane);
+        ci = *cluster.map_shared_rank(&cand_i[par], lane);
+      }
+      warp_argmax_first_f(cv, ci);
+      if (lane == 0) s_p = (ci == INT_MAX) ? kk : ci;
+    }
+    __syncthreads();
+    const int p = s_p;
+    const int own_p = p / R, loc_p = p - own_p * R;
+    const int own_k = kk / R, loc_k = kk - own_k * R;
+    if (tid < kLu32NB) {
+      rowp[tid] = cluster.map_shared_rank(P, own_p)[loc_p * kPanelLd + tid];
+    } else if (tid < 2 * kLu32NB) {
+      rowk[tid - kLu32NB] = cluster.map_shared_rank(P, own_k)[loc_k * kPanelLd + tid - kLu32NB];
+    }
+    cluster.sync();
+    const float akk = rowp[kk];
+    if (akk != 0.0f && p != kk) {
+      if (rank == own_k && tid < kLu32NB) P[loc_k * kPanelLd + tid] = rowp[tid];
+      if (rank == own_p && tid < kLu32NB) P[loc_p * kPanelLd + tid] = rowk[tid];
+    }
+    if (rank == 0 && tid == 0) {
+      piv[j0 + kk] = j0 + p;
+      if (akk == 0.0f && *info == 0) *info = j0 + kk + 1;
+    }
+    __syncthreads();
+    const float rcp = (akk != 0.0f) ? 1.0f / akk : 0.0f;
+    for (int i = tid; i < mloc; i += blockDim.x) {
+      if (r0 + i > kk) {
+        float* row = P + i * kPanelLd;
+        float l = row[kk];
+        if (akk != 0.0f) {
+          l *= rcp;
+          row[kk] = l;
+        }
+        for (int j = kk + 1; j < nb; ++j) row[j] = fmaf(-l, rowp[j], row[j]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < mloc * kLu32NB; e += blockDim.x) {
+    const int i = e / kLu32NB, j = e % kLu32NB;
+    if (j < nb) a[(int64_t)(j0 + r0 + i) * n + j0 + j] = P[i * kPanelLd + j];
+  }
+}
+
+// Cluster geometry for an m-row panel: 0 when it does not fit (or the device
+// cannot co-schedule the cluster), else the CTA count (rows_per_cta set).
+static int panel_cluster_size(int m, int* rows_per_cta) {
+  int c = (m + kPanelCluThreads - 1) / kPanelCluThreads;
+  c = c < 1 ? 1 : (c > kPanelCluMax ? kPanelCluMax : c);
+  const int r = (m + c - 1) / c;
+  if ((size_t)r * kPanelLd * sizeof(float) > kPanelCluSmemMax) return 0;
+  *rows_per_cta = r;
+  return c;
+}
+
+static int launch_panel_cluster(int n, int j0, int nb, float* a, int32_t* piv, int32_t* info,
+                                cudaStream_t st) {
+  int r = 0;
+  const int c = panel_cluster_size(n - j0, &r);
+  if (c == 0) return -1;
+  const size_t smem = (size_t)r * kPanelLd * sizeof(float);
+  if (cudaFuncSetAttribute(panel_getf2_cluster_kernel,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(panel_getf2_cluster_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c);
+  cfg.blockDim = dim3(kPanelCluThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)c;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, panel_getf2_cluster_kernel, &cfg) != cudaSuccess ||
+      nclusters < 1) {
+    cudaGetLastError();
+    return -1;
+  }
+  if (cudaLaunchKernelEx(&cfg, panel_getf2_cluster_kernel, n, j0, nb, r, a, piv, info) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return 0;
+}
+
 __global__ void laswp_f32_kernel(int n, int j0, int nb, float* __restrict__ a,
                                  const int32_t* __restrict__ piv) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,47 +275,6 @@ __global__ void laswp_f32_kernel(int n, int j0, int nb, float* __restrict__ a,
       a[(int64_t)k * n + j] = a[(int64_t)p * n + j];
       a[(int64_t)p * n + j] = t;
     }
-  }
-}
-
-// U12 = L11^{-1} A12, one column per thread (column-oriented substitution).
-__global__ void __launch_bounds__(128)
-trsm_blockrow_f32_kernel(int n, int j0, int nb, float* __restrict__ a) {
-  __shared__ float L[kLu32NB][kLu32NB + 1];
-  for (int e = threadIdx.x; e < kLu32NB * kLu32NB; e += blockDim.x) {
-    const int i = e / kLu32NB, k = e % kLu32NB;
-    L[i][k] = (i < nb && k < nb) ? a[(int64_t)(j0 + i) * n + j0 + k] : 0.0f;
-  }
-  __syncthreads();
-  const int j = j0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  float col[kLu32NB];
-#pragma unroll
-  for (int i = 0; i < kLu32NB; ++i) col[i] = (i < nb) ? a[(int64_t)(j0 + i) * n + j] : 0.0f;
-#pragma unroll
-  for (int k = 0; k < kLu32NB; ++k) {
-#pragma unroll
-    for (int i = k + 1; i < kLu32NB; ++i) col[i] = fmaf(-L[i][k], col[k], col[i]);
-  }
-#pragma unroll
-  for (int i = 0; i < kLu32NB; ++i)
-    if (i < nb) a[(int64_t)(j0 + i) * n + j] = col[i];
-}
-
-// bt[j][p] = a[j0+p][j0+nb+j]  (U12ᵀ, K-major for the GEMM), ld of bt = kLu32NB.
-__global__ void transpose_u12_kernel(int n, int j0, int nb, const float* __restrict__ a,
-                                     float* __restrict__ bt) {
-  __shared__ float tile[32][33];
-  const int jb = blockIdx.x * 32, pb = blockIdx.y * 32;
-  const int n2 = n - j0 - nb;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int p = pb + r, j = jb + threadIdx.x;
-    tile[r][threadIdx.x] = (p < nb && j < n2) ? a[(int64_t)(j0 + p) * n + j0 + nb + j] : 0.0f;
-  }
-  __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int j = jb + r, p = pb + threadIdx.x;
-    if (j < n2) bt[(int64_t)j * kLu32NB + p] = tile[threadIdx.x][r];
   }
 }
 
@@ -227,14 +352,15 @@ extern "C" int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_
   float* bl = reinterpret_cast<float*>(wb + 4 * blk);
   for (int j0 = 0; j0 < n; j0 += kLu32NB) {
     const int nb = min(kLu32NB, n - j0);
-    panel_getf2_f32_kernel<<<1, kLu32PanelThreads, 0, st>>>(n, j0, nb, lu, piv, info);
+    if (launch_panel_cluster(n, j0, nb, lu, piv, info, st) != 0)
+      panel_getf2_f32_kernel<<<1, kLu32PanelThreads, 0, st>>>(n, j0, nb, lu, piv, info);
     const int outside = n - nb;
     if (outside > 0) laswp_f32_kernel<<<(outside + 127) / 128, 128, 0, st>>>(n, j0, nb, lu, piv);
     const int n2 = n - j0 - nb;
     if (n2 > 0) {
-      trsm_blockrow_f32_kernel<<<(n2 + 127) / 128, 128, 0, st>>>(n, j0, nb, lu);
-      dim3 tg((unsigned)((n2 + 31) / 32), (unsigned)((nb + 31) / 32));
-      transpose_u12_kernel<<<tg, dim3(32, 8), 0, st>>>(n, j0, nb, lu, bt);
+      // U12 = L11^{-1} A12 in place, and U12ᵀ (K-major) into bt for the GEMM
+      int rc0 = launch_inv_diag_lower(n, j0, nb, lu, lu, j0 + nb, n, bt, st);
+      if (rc0) return rc0;
       // A22 -= L21 U12   (A = L21: n2×nb at lu[(j0+nb)*n + j0], B = U12ᵀ: n2×nb)
       float* c22 = lu + (int64_t)(j0 + nb) * n + j0 + nb;
       const float* l21 = lu + (int64_t)(j0 + nb) * n + j0;

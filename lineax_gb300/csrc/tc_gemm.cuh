@@ -11,6 +11,13 @@ int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* 
 int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int64_t lda,
                        const float* B, const float* Bl, int64_t ldb, float* C, int64_t ldc,
                        float alpha, float beta, int* err, cudaStream_t st);
+// X = L_jj^{-1} W on rows [j0, j0+nb) of w, columns [c_begin, c_end), L_jj
+// the unit-lower 64-block of lu at (j0, j0) (row stride n; lu and w may be
+// the same array when the columns are disjoint from the block).  X goes back
+// into w and, transposed and zero padded to 64 entries per column, into xt
+// (ir.cu).
+int launch_inv_diag_lower(int n, int j0, int nb, const float* lu, float* w, int c_begin,
+                          int c_end, float* xt, cudaStream_t st);
 // hi/lo split of a rows×cols block (row stride lds) into hi, lo (row stride ldd).
 int tf32_split(int64_t rows, int64_t cols, const float* src, int64_t lds, float* hi, float* lo,
                int64_t ldd, cudaStream_t st);

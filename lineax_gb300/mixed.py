@@ -2,8 +2,14 @@
 
 The factor is computed in FP32 with partial pivoting and tensor-core (TF32)
 trailing updates (lxgb_getrf_f32_tc); FP64 GMRES on the original operator,
-left-preconditioned by the FP32 LU solve, recovers FP64 accuracy (GMRES-based
-iterative refinement, Carson & Higham 2017).  Through the lineax API this is
+left-preconditioned by the FP32 LU, recovers FP64 accuracy (GMRES-based
+iterative refinement, Carson & Higham 2017).  The preconditioner is applied
+as M x = U^{-1} (L^{-1} (P x)) with the triangular inverses formed once on
+the tensor cores (lxgb_lu32_inverse): two matrix-vector products that spread
+over every SM, in double-float arithmetic so that M stays one fixed linear
+operator to FP64 accuracy however ill-conditioned the factor is (the
+preconditioner precision u_p of five-precision GMRES-IR, Amestoy et al.
+2023).  Through the lineax API this is
 
     M = lu_preconditioner(operator)
     lx.linear_solve(operator, b, lx.GMRES(rtol, atol, restart=20),
@@ -92,10 +98,139 @@ class LUPreconditioner(AbstractLinearOperator):  # noqa: D101
         return self._s
 
 
-def lu_preconditioner(operator, precision: str = "3xtf32") -> LUPreconditioner:
-    """FP32 LU (tensor-core updates) of the operator's matrix as a GMRES preconditioner."""
+ARITH = {"fp32": 0, "df": 1}
+
+
+@dataclasses.dataclass
+class InverseLU32:
+    linv: torch.Tensor  # L^{-1}, n×n FP32 (unit lower, zeros above the diagonal)
+    uinv: torch.Tensor  # U^{-1}, n×n FP32 (zeros below the diagonal)
+    perm: torch.Tensor  # (P b)_i = b[perm[i]]
+
+
+def lu_inverse(factor: LU32, precision: str = "3xtf32") -> InverseLU32:
+    """Triangular inverses of an FP32 LU, off-diagonal blocks on the tensor cores."""
+    lu = factor.lu
+    n = lu.shape[0]
+    dev = lu.device
+    linv = torch.empty((n, n), dtype=torch.float32, device=dev)
+    uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    prec = PRECISIONS[precision]
+    wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, prec))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(lu), _ffi.ptr(factor.piv), _ffi.ptr(linv),
+              _ffi.ptr(uinv), _ffi.ptr(perm), prec, _ffi.ptr(err), _ffi.ptr(work),
+              work.numel() * 8, _ffi.stream_handle(dev))
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
+    return InverseLU32(linv, uinv, perm)
+
+
+class _BlockOperator(AbstractLinearOperator):
+    """Square n×n FP64 operator defined by a (k, n) block product."""
+
+    def __init__(self, n: int):
+        self._s = ShapeDtypeStruct((n,), torch.float64)
+        self.tags = frozenset()
+
+    def mv(self, vector):
+        return self.mv_block(vector.reshape(1, -1)).reshape(vector.shape)
+
+    def as_matrix(self):
+        raise NotImplementedError("matrix-free operator")
+
+    def transpose(self):
+        raise NotImplementedError("transpose not provided")
+
+    def in_structure(self):
+        return self._s
+
+    def out_structure(self):
+        return self._s
+
+
+class InverseLUPreconditioner(_BlockOperator):
+    """M = U^{-1} L^{-1} P from the triangular inverses of an FP32 LU, applied
+    in "df" (double-float, FP64-accurate) or "fp32" arithmetic."""
+
+    def __init__(self, factor: LU32, inverse: InverseLU32, arith: str = "df"):
+        super().__init__(inverse.linv.shape[0])
+        self.factor = factor
+        self.inverse = inverse
+        self.mode = ARITH[arith]
+        self._work = None
+
+    def mv_block(self, x: torch.Tensor) -> torch.Tensor:
+        xb = as_device_f64(x).contiguous()
+        k, n = xb.shape
+        out = torch.empty_like(xb)
+        wbytes = int(_ffi.load().lxgb_lu32_apply_workspace_size(n, k))
+        if self._work is None or self._work.numel() * 8 < wbytes:
+            self._work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=xb.device)
+        inv = self.inverse
+        _ffi.call("lxgb_lu32_apply", n, k, _ffi.ptr(inv.linv), _ffi.ptr(inv.uinv),
+                  _ffi.ptr(inv.perm), self.mode, _ffi.ptr(xb), _ffi.ptr(out),
+                  _ffi.ptr(self._work), self._work.numel() * 8, _ffi.stream_handle(xb.device))
+        return out
+
+
+@dataclasses.dataclass
+class SplitMatrix:
+    hi: torch.Tensor  # A truncated to 24 significant bits (FP32)
+    lo: torch.Tensor  # the next 24 bits (FP32)
+
+
+def split_matrix(a: torch.Tensor) -> SplitMatrix:
+    """A (FP64) as an FP32 hi + lo pair: 48 significant bits."""
+    a64 = as_device_f64(a)
+    m, n = a64.shape
+    hi = torch.empty((m, n), dtype=torch.float32, device=a64.device)
+    lo = torch.empty_like(hi)
+    _ffi.call("lxgb_split_f64", m, n, _ffi.ptr(a64), a64.stride(0), _ffi.ptr(hi), _ffi.ptr(lo), n,
+              _ffi.stream_handle(a64.device))
+    return SplitMatrix(hi, lo)
+
+
+class SplitMatrixOperator(_BlockOperator):
+    """A x with A held as a SplitMatrix: "df" gives FP64-accurate products in
+    double-float arithmetic on the FP32 pipe, "fp32" uses the hi part in FP32."""
+
+    def __init__(self, split: SplitMatrix, arith: str = "df"):
+        super().__init__(split.hi.shape[0])
+        self.split = split
+        self.mode = ARITH[arith]
+        self._work = None
+
+    def _run(self, x: torch.Tensor, b: torch.Tensor | None) -> torch.Tensor:
+        xb = as_device_f64(x).contiguous()
+        k, n = xb.shape
+        out = torch.empty_like(xb)
+        wbytes = int(_ffi.load().lxgb_gemv_df_workspace_size(n, k))
+        if self._work is None or self._work.numel() * 8 < wbytes:
+            self._work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=xb.device)
+        lo = self.split.lo if self.mode == 1 else None
+        _ffi.call("lxgb_gemv_df", n, n, _ffi.ptr(self.split.hi), _ffi.ptr(lo), n, k, _ffi.ptr(xb),
+                  n, _ffi.ptr(b), _ffi.ptr(out), n, self.mode, _ffi.ptr(self._work),
+                  self._work.numel() * 8, _ffi.stream_handle(xb.device))
+        return out
+
+    def mv_block(self, x: torch.Tensor) -> torch.Tensor:
+        return self._run(x, None)
+
+    def residual(self, x: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+        """b - A x for (k, n) blocks."""
+        return self._run(x, as_device_f64(b).contiguous())
+
+
+def lu_preconditioner(operator, precision: str = "3xtf32", arith: str = "df"
+                      ) -> InverseLUPreconditioner:
+    """FP32 LU (tensor-core updates) of the operator's matrix as a GMRES
+    preconditioner, applied through its triangular inverses."""
     mat = operator.matrix if isinstance(operator, MatrixLinearOperator) else operator.as_matrix()
-    return LUPreconditioner(lu_factor_tf32(mat, precision))
+    f = lu_factor_tf32(mat, precision)
+    return InverseLUPreconditioner(f, lu_inverse(f, precision), arith)
 
 
 def _kmax(x: torch.Tensor) -> torch.Tensor:
@@ -128,49 +263,85 @@ class IRResult:
     outer: int               # refinement steps
     inner_steps: list        # GMRES outer iterations (restart cycles) per refinement step
     converged: bool
+    fallback: bool = False   # solved by the FP64 LU after GMRES-IR stalled
 
 
 def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol: float = 1e-6,
              restart: int = 20, stagnation_iters: int = 20, max_outer: int = 20,
-             factor: LU32 | None = None, precision: str = "3xtf32") -> IRResult:
+             inner_max_steps: int | None = None, factor: LU32 | None = None,
+             inverse: InverseLU32 | None = None, split: SplitMatrix | None = None,
+             precision: str = "3xtf32", arith: str = "df", fallback: bool = False) -> IRResult:
     """GMRES-based iterative refinement for A X = B (B: (k, n) FP64).
 
-    Each refinement step solves A d = r / ||r||_inf with FP64 GMRES (lineax
-    semantics, rtol = atol = inner_rtol) left-preconditioned by the FP32/TF32
-    LU, then x += ||r||_inf d and r = b - A x in FP64, until the normwise
-    backward error of every right-hand side is <= tol."""
+    Each refinement step solves A d = r / ||r||_inf with GMRES (lineax
+    semantics, rtol = atol = inner_rtol) left-preconditioned by the FP32 LU,
+    then x += ||r||_inf d and r = b - A x, until the normwise backward error
+    of every right-hand side is <= tol.  arith "df" runs the inner operator
+    and preconditioner products in double-float (FP64-accurate) arithmetic,
+    "fp32" in FP32 (classic mixed-precision refinement); the outer residual is
+    always FP64-accurate (A as a 48-bit hi + lo pair, double-float sums).
+
+    fallback=True stops refining as soon as it stalls (an inner solve that
+    does not reach inner_rtol, or a refinement step that shrinks the largest
+    backward error by less than 2x) and solves with the FP64 LU instead, as
+    mixed-precision solvers do when the low-precision factor is too far from
+    A (kappa(A) u_f well above 1): IRResult.fallback is then True."""
     a64 = as_device_f64(a)
     b64 = as_device_f64(b)
     if b64.ndim == 1:
         b64 = b64.reshape(1, -1)
+    b64 = b64.contiguous()
     k, n = b64.shape
-    dev = a64.device
-    st = _ffi.stream_handle(dev)
     if factor is None:
         factor = lu_factor_tf32(a64, precision)
-    op = MatrixLinearOperator(a64)
-    pre = LUPreconditioner(factor)
+    if inverse is None:
+        inverse = lu_inverse(factor, precision)
+    if split is None:
+        split = split_matrix(a64)
+    outer_op = SplitMatrixOperator(split, "df")
+    inner_op = outer_op if arith == "df" else SplitMatrixOperator(split, arith)
+    pre = InverseLUPreconditioner(factor, inverse, arith)
     anorm = float(norm_inf(a64).item())
     bnorm = _kmax(b64).cpu()
     x = torch.zeros_like(b64)
     r = b64.clone()
+    st = _ffi.stream_handle(a64.device)
     inner_steps, berr, converged, it = [], [float("inf")] * k, False, 0
     for it in range(1, max_outer + 1):
         rn = _kmax(r)
         rhat = r.clone()
         _ffi.call("lxgb_rows_scale_f64", k, n, _ffi.ptr(rn), 1, _ffi.ptr(rhat), st)
-        res = _krylov.gmres_block(op, rhat, rtol=inner_rtol, atol=inner_rtol, restart=restart,
-                                  stagnation_iters=stagnation_iters, preconditioner=pre)
+        res = _krylov.gmres_block(inner_op, rhat, rtol=inner_rtol, atol=inner_rtol,
+                                  restart=restart, stagnation_iters=stagnation_iters,
+                                  max_steps=inner_max_steps, preconditioner=pre)
         inner_steps.append(max(res.steps))
         _ffi.call("lxgb_rows_axpy_f64", k, n, _ffi.ptr(rn), _ffi.ptr(res.y), _ffi.ptr(x), st)
-        r.copy_(b64)
-        _ffi.call("lxgb_gemv_f64", n, n, _ffi.ptr(a64), n, 0, k, _ffi.ptr(x), n, _ffi.ptr(r), n,
-                  -1.0, 1.0, st)
-        rn_h = _kmax(r).cpu()
-        xn_h = _kmax(x).cpu()
-        berr = [float(rn_h[c] / (anorm * xn_h[c] + bnorm[c])) if (anorm * xn_h[c] + bnorm[c]) > 0
-                else 0.0 for c in range(k)]
+        r = outer_op.residual(x, b64)
+        prev = max(berr)
+        berr = _berr(r, x, anorm, bnorm)
         if all(e <= tol for e in berr):
             converged = True
             break
+        stalled = any(code != _krylov.SUCCESSFUL for code in res.results) or max(berr) > prev / 2
+        if fallback and stalled:
+            return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
+    if fallback and not converged:
+        return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
     return IRResult(x, berr, it, inner_steps, converged)
+
+
+def _berr(r, x, anorm, bnorm) -> list:
+    rn_h = _kmax(r).cpu()
+    xn_h = _kmax(x).cpu()
+    return [float(rn_h[c] / (anorm * xn_h[c] + bnorm[c])) if (anorm * xn_h[c] + bnorm[c]) > 0
+            else 0.0 for c in range(r.shape[0])]
+
+
+def _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps) -> IRResult:
+    """FP64 LU solve (lxgb_getrf/getrs) after GMRES-IR stalled."""
+    from . import _dense
+
+    lu, piv = _dense.lu_factor(a64)
+    x = _dense.lu_solve(lu, piv, b64)
+    berr = _berr(outer_op.residual(x, b64), x, anorm, bnorm)
+    return IRResult(x, berr, it, inner_steps, all(e <= tol for e in berr), fallback=True)

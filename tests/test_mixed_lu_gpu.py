@@ -26,7 +26,7 @@ def conditioned(n, cond, seed):
 
 
 @pytest.mark.parametrize("precision,bound", [("tf32", 3e-2), ("3xtf32", 5e-5)])
-@pytest.mark.parametrize("n", [64, 256, 600, 1024])
+@pytest.mark.parametrize("n", [64, 256, 600, 1024, 2500])
 def test_tf32_lu_factorisation_residual(dev, n, precision, bound):
     """||P A - L U|| / ||A||: TF32 products leave a few units of sqrt(n) 2^-11;
     3xTF32 is at FP32 level."""
@@ -44,18 +44,114 @@ def test_tf32_lu_factorisation_residual(dev, n, precision, bound):
     assert rel < bound, rel
 
 
-@pytest.mark.parametrize("n,cond", [(256, 1e2), (512, 1e6), (1024, 1e2), (1024, 1e6)])
-def test_gmres_ir_reaches_fp64_backward_error(dev, n, cond):
+def swaps_to_perm(piv):
+    perm = np.arange(len(piv))
+    for k, p in enumerate(piv):
+        perm[[k, p]] = perm[[p, k]]
+    return perm
+
+
+@pytest.mark.parametrize("precision,ulp", [("tf32", 2.0 ** -11), ("3xtf32", 2.0 ** -22)])
+@pytest.mark.parametrize("n", [256, 600, 1024])
+def test_lu_inverse_factors(dev, n, precision, ulp):
+    """L^{-1} L = I and U^{-1} U = I componentwise to the update's rounding:
+    |X T - I| <= n u |X| |T| (TF32 u = 2^-11, 3xTF32 about 2^-22); perm
+    composes the row interchanges."""
+    a = conditioned(n, 1e2, n + 1)
+    f = mixed.lu_factor_tf32(torch.tensor(a, device=dev), precision)
+    inv = mixed.lu_inverse(f, precision)
+    lu = f.lu.double().cpu().numpy()
+    l = np.tril(lu, -1) + np.eye(n)
+    u = np.triu(lu)
+    linv = inv.linv.double().cpu().numpy()
+    uinv = inv.uinv.double().cpu().numpy()
+    assert np.all(np.triu(linv, 1) == 0) and np.all(np.diag(linv) == 1)
+    assert np.all(np.tril(uinv, -1) == 0)
+    for x, t in ((linv, l), (uinv, u)):
+        scale = np.abs(x) @ np.abs(t)
+        err = np.abs(x @ t - np.eye(n))
+        assert np.all(err[scale == 0] == 0)
+        assert np.max(err[scale > 0] / scale[scale > 0]) < n * ulp
+    assert np.array_equal(inv.perm.cpu().numpy(), swaps_to_perm(f.piv.cpu().numpy()))
+
+
+@pytest.mark.parametrize("arith,bound", [("df", 1e-13), ("fp32", 1e-5)])
+@pytest.mark.parametrize("n,k", [(256, 1), (600, 16), (1024, 20)])
+def test_inverse_preconditioner_apply(dev, n, k, arith, bound):
+    """M x = U^{-1} (L^{-1} (P x)) against the same FP32 inverses applied in FP64."""
+    a = conditioned(n, 1e6, n + 2)
+    f = mixed.lu_factor_tf32(torch.tensor(a, device=dev), "3xtf32")
+    inv = mixed.lu_inverse(f, "3xtf32")
+    x = np.random.default_rng(n + k).standard_normal((k, n))
+    m = mixed.InverseLUPreconditioner(f, inv, arith)
+    y = m.mv_block(torch.tensor(x, device=dev)).cpu().numpy()
+    linv = inv.linv.double().cpu().numpy()
+    uinv = inv.uinv.double().cpu().numpy()
+    perm = inv.perm.cpu().numpy()
+    ref = (uinv @ (linv @ x[:, perm].T)).T
+    scale = (np.abs(uinv) @ (np.abs(linv) @ np.abs(x[:, perm]).T)).T
+    assert np.max(np.abs(y - ref) / scale) < bound
+
+
+@pytest.mark.parametrize("m,n,k", [(300, 200, 5), (512, 512, 16), (129, 700, 20)])
+def test_double_float_gemv(dev, m, n, k):
+    """A x and b - A x with A as an FP32 hi + lo pair: FP64-level accuracy in
+    double-float, FP32-level on the hi part alone."""
+    rng = np.random.default_rng(m + n + k)
+    a = rng.standard_normal((m, n))
+    x = rng.standard_normal((k, n))
+    b = rng.standard_normal((k, m))
+    at = torch.tensor(a, device=dev)
+    sp = mixed.split_matrix(at)
+    assert np.abs(sp.hi.double().cpu().numpy() + sp.lo.double().cpu().numpy() - a).max() \
+        <= 2.0 ** -46 * np.abs(a).max()
+    lib_y = torch.empty((k, m), dtype=torch.float64, device=dev)
+    from lineax_gb300 import _ffi
+    wb = int(_ffi.load().lxgb_gemv_df_workspace_size(n, k))
+    work = torch.empty(wb // 8 + 1, dtype=torch.float64, device=dev)
+    xt = torch.tensor(x, device=dev)
+    bt = torch.tensor(b, device=dev)
+    scale = np.abs(x) @ np.abs(a).T
+    for mode, bound in ((1, 1e-14), (0, 1e-6)):
+        lo = sp.lo if mode == 1 else None
+        for with_b in (False, True):
+            _ffi.call("lxgb_gemv_df", m, n, _ffi.ptr(sp.hi), _ffi.ptr(lo), n, k, _ffi.ptr(xt), n,
+                      _ffi.ptr(bt if with_b else None), _ffi.ptr(lib_y), m, mode, _ffi.ptr(work),
+                      work.numel() * 8, _ffi.stream_handle(dev))
+            y = lib_y.cpu().numpy()
+            ref = (b - x @ a.T) if with_b else x @ a.T
+            assert np.max(np.abs(y - ref) / scale) < bound, (mode, with_b)
+
+
+@pytest.mark.parametrize("n,cond,arith", [(256, 1e2, "df"), (512, 1e6, "df"), (1024, 1e2, "df"),
+                                          (1024, 1e6, "df"), (512, 1e2, "fp32")])
+def test_gmres_ir_reaches_fp64_backward_error(dev, n, cond, arith):
     a = conditioned(n, cond, n + int(np.log10(cond)))
     rng = np.random.default_rng(7)
     b = rng.standard_normal((4, n))
-    res = mixed.gmres_ir(torch.tensor(a, device=dev), torch.tensor(b, device=dev), tol=1e-12)
-    assert res.converged and res.outer <= 6, (res.outer, res.berr)
+    res = mixed.gmres_ir(torch.tensor(a, device=dev), torch.tensor(b, device=dev), tol=1e-12,
+                         arith=arith)
+    assert res.converged and not res.fallback and res.outer <= 6, (res.outer, res.berr)
     x = res.x.cpu().numpy()
     for c in range(4):
         assert res.berr[c] <= 1e-12
         assert dense.backward_error(a, x[c], b[c]) <= 1e-12
         assert dense.forward_error(x[c], dense.lu_linear_solve(a, b[c])) <= cond * 1e-13
+
+
+def test_gmres_ir_falls_back_to_fp64_when_it_stalls(dev):
+    """cond 1e10 with log-spaced singular values leaves about a quarter of the
+    directions below FP32 resolution: GMRES(20) stalls, and fallback=True
+    returns the FP64 LU solution instead."""
+    n = 512
+    a = conditioned(n, 1e10, 99)
+    b = np.random.default_rng(5).standard_normal((3, n))
+    res = mixed.gmres_ir(torch.tensor(a, device=dev), torch.tensor(b, device=dev), tol=1e-12,
+                         max_outer=4, inner_max_steps=10, fallback=True)
+    assert res.fallback and res.converged, res.berr
+    x = res.x.cpu().numpy()
+    for c in range(3):
+        assert dense.backward_error(a, x[c], b[c]) <= 1e-12
 
 
 def test_gmres_ir_through_linear_solve(dev):
@@ -74,10 +170,10 @@ def test_gmres_ir_through_linear_solve(dev):
     lu = m.factor.lu.cpu().numpy()
     piv = m.factor.piv.cpu().numpy()
 
-    def pre(v):  # the FP32 factor applied in FP32, as on the device
+    def pre(v):  # the FP32 factor applied in FP64 (the device applies its inverses in double-float)
         import scipy.linalg as sl
-        return sl.lu_solve((lu, piv), v.astype(np.float32)).astype(np.float64)
+        return sl.lu_solve((lu.astype(np.float64), piv), v)
 
     x_ref, r_ref, s_ref = krylov.gmres(lambda v: a @ v, b, rtol=1e-10, atol=1e-10, precond=pre)
-    # FP32 preconditioner applies differ in rounding order: allow two restart cycles
+    # The inverses carry FP32 rounding of their own: allow two restart cycles
     assert r_ref == 0 and abs(sol.stats["num_steps"] - s_ref) <= 2
