@@ -446,11 +446,11 @@ def run_gmres_ir(args):
     lu0, piv0 = _dense.lu_factor(a0)
     _dense.lu_solve(lu0, piv0, b[:, :256].contiguous())
     torch.cuda.synchronize()
-    for cond in (1e2, 1e6, 1e10):
+    for cond in [float(c) for c in args.conds.split(",")]:
         a = haar_conditioned(n, cond, 5, dev)
         anorm = float(mixed.norm_inf(a).item())
         bn = b.abs().amax(dim=1)
-        if cond == 1e2 or args.fp64_all:
+        if (cond == 1e2 or args.fp64_all) and not args.no_fp64:
             e0, e1, e2 = ev(), ev(), ev()
             e0.record()
             lu, piv = _dense.lu_factor(a)
@@ -465,7 +465,7 @@ def run_gmres_ir(args):
                   "max_berr": berr, "solves_per_s": k / (e0.elapsed_time(e2) * 1e-3)})
             del lu, x
             torch.cuda.empty_cache()
-        for prec in ("tf32", "3xtf32"):
+        for prec in args.precisions.split(","):
             t0 = time.perf_counter()
             e = [ev() for _ in range(5)]
             e[0].record()
@@ -475,13 +475,14 @@ def run_gmres_ir(args):
             e[2].record()
             sp = mixed.split_matrix(a)
             e[3].record()
-            res = mixed.gmres_ir(a, b, tol=1e-12, restart=args.restart, max_outer=10,
+            res = mixed.gmres_ir(a, b, tol=1e-12, restart=args.restart, max_outer=20,
                                  inner_max_steps=args.inner_max_steps, factor=f, inverse=inv,
-                                 split=sp, precision=prec, arith="df", fallback=True)
+                                 split=sp, precision=prec, arith=args.arith, fallback=True)
             e[4].record()
             torch.cuda.synchronize()
             total = e[0].elapsed_time(e[4])
             emit({"case": f"gmres_ir_{prec}", "cond": cond, "restart": args.restart,
+                  "arith": args.arith,
                   "factor_ms": e[0].elapsed_time(e[1]), "inverse_ms": e[1].elapsed_time(e[2]),
                   "split_ms": e[2].elapsed_time(e[3]), "refine_ms": e[3].elapsed_time(e[4]),
                   "total_ms": total, "outer": res.outer, "inner_cycles": res.inner_steps,
@@ -508,9 +509,14 @@ def main():
                    choices=["ragged_cholesky", "gmres_ir"],
                    help="gmres_ir: the dense mixed-precision LU + GMRES-IR workload")
     p.add_argument("--n", type=int, default=8192, help="order for --workload gmres_ir")
-    p.add_argument("--restart", type=int, default=20, help="GMRES restart for --workload gmres_ir")
-    p.add_argument("--inner-max-steps", type=int, default=20,
+    p.add_argument("--restart", type=int, default=8, help="GMRES restart for --workload gmres_ir")
+    p.add_argument("--inner-max-steps", type=int, default=5,
                    help="GMRES restart cycles per refinement step before falling back to FP64")
+    p.add_argument("--conds", default="1e2,1e6,1e10", help="condition numbers (gmres_ir)")
+    p.add_argument("--arith", default="auto", choices=["auto", "df", "fp32"],
+                   help="inner GMRES arithmetic (gmres_ir)")
+    p.add_argument("--precisions", default="tf32,3xtf32", help="factor precisions (gmres_ir)")
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 LU line (gmres_ir)")
     p.add_argument("--fp64-all", action="store_true",
                    help="time the plain FP64 LU at every condition number (gmres_ir)")
     args = p.parse_args()

@@ -42,9 +42,16 @@ struct TcSmem {
   alignas(8) unsigned long long full[S];
   alignas(8) unsigned long long empty[S];
   alignas(8) unsigned long long done;
+  alignas(8) unsigned long long cfull;  // old C tile landed (TMA epilogue)
   unsigned tmem_base;
   int abort;
 };
+
+// The TMA epilogue stages the 128×128 FP32 C tile (64 KB) in the stage buffers.
+static_assert(sizeof(TcSmem<kTcStages, false>::a) + sizeof(TcSmem<kTcStages, false>::b) >=
+                  4 * kTcTileBytes, "C tile does not fit the TF32 stage buffers");
+static_assert(sizeof(TcSmem<kTcStagesSplit, true>::a) + sizeof(TcSmem<kTcStagesSplit, true>::b) >=
+                  4 * kTcTileBytes, "C tile does not fit the 3xTF32 stage buffers");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -121,6 +128,13 @@ __device__ __forceinline__ void mma_commit(unsigned long long* bar) {
       : "memory");
 }
 
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<unsigned long long>(map)),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
   unsigned r[32];
   asm volatile(
@@ -146,8 +160,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
                     const __grid_constant__ CUtensorMap map_b,
                     const __grid_constant__ CUtensorMap map_al,
-                    const __grid_constant__ CUtensorMap map_bl, int M, int N, int K, float* C,
-                    int64_t ldc, float alpha, float beta, int* err) {
+                    const __grid_constant__ CUtensorMap map_bl,
+                    const __grid_constant__ CUtensorMap map_c, int use_tma_c, int M, int N, int K,
+                    float* C, int64_t ldc, float alpha, float beta, int* err) {
   constexpr int kStages = SPLIT ? kTcStagesSplit : kTcStages;
   using Smem = TcSmem<kStages, SPLIT>;
   extern __shared__ unsigned char smem_raw[];
@@ -163,6 +178,7 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
       mbar_init(&sm.empty[s], 1);
     }
     mbar_init(&sm.done, 1);
+    mbar_init(&sm.cfull, 1);
     sm.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -226,8 +242,59 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!done_ok || sm.abort) {
     if (threadIdx.x == 0) atomicExch(err, 1);
-  } else {
-    // Epilogue: warp w owns rows 32w..32w+31 (TMEM lanes), 32 columns per load.
+  } else if (use_tma_c) {
+    // Epilogue through shared memory: the old C tile arrives by TMA into the
+    // (now idle) stage buffers as four 128-row × 32-column boxes with the
+    // 128-byte swizzle, each thread updates its row in place (16-byte granule
+    // g of row r sits at g ^ (r & 7): conflict-free), and TMA stores the tile
+    // (rows and columns past M, N are clipped by the tensor map).
+    float* cbuf = &sm.a[0][0];  // 64 KB: a[] and, for 3 stages, b[0] follow contiguously
+    const bool has_acc = ktiles > 0;
+    bool c_ok = true;
+    if (beta != 0.0f) {
+      if (threadIdx.x == 0) {
+        mbar_expect_tx(&sm.cfull, 4 * kTcTileBytes);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) tma_load_2d(cbuf + i * kTcM * kTcK, &map_c, n0 + 32 * i, m0,
+                                                &sm.cfull);
+      }
+      c_ok = mbar_wait(&sm.cfull, 0);
+    }
+    if (!c_ok) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+    } else {
+      const int r = warp * 32 + lane;
+#pragma unroll 1
+      for (int i = 0; i < 4; ++i) {
+        float v[32];
+        if (has_acc) {
+          tmem_ld32(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(32 * i), v);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 32; ++e) v[e] = 0.0f;
+        }
+        char* rowp = reinterpret_cast<char*>(cbuf + i * kTcM * kTcK) + r * 128;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          float4* q = reinterpret_cast<float4*>(rowp + ((g ^ (r & 7)) << 4));
+          float4 o = (beta != 0.0f) ? *q : make_float4(0.f, 0.f, 0.f, 0.f);
+          o.x = fmaf(alpha, v[4 * g + 0], beta == 0.0f ? 0.0f : beta * o.x);
+          o.y = fmaf(alpha, v[4 * g + 1], beta == 0.0f ? 0.0f : beta * o.y);
+          o.z = fmaf(alpha, v[4 * g + 2], beta == 0.0f ? 0.0f : beta * o.z);
+          o.w = fmaf(alpha, v[4 * g + 3], beta == 0.0f ? 0.0f : beta * o.w);
+          *q = o;
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (c_ok && threadIdx.x == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) tma_store_2d(&map_c, n0 + 32 * i, m0, cbuf + i * kTcM * kTcK);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+  } else {    // Epilogue: warp w owns rows 32w..32w+31 (TMEM lanes), 32 columns per load.
     const int row = m0 + warp * 32 + lane;
     const bool has_acc = ktiles > 0;
 #pragma unroll 1
@@ -323,21 +390,28 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
     rc = make_map(&mbl, Bl, N, K, ldb);
     if (rc) return rc;
   }
+  // TMA epilogue when C meets the tensor-map rules (16-byte base and row stride)
+  CUtensorMap mc = ma;
+  int use_tma_c = 0;
+  if ((((uintptr_t)C) & 15) == 0 && (ldc % 4) == 0 && make_map(&mc, C, M, N, ldc) == 0)
+    use_tma_c = 1;
+  else
+    cudaGetLastError();
   dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
   if (split) {
     const size_t smem = sizeof(TcSmem<kTcStagesSplit, true>) + 1024;
     LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                   "gemm_tf32: set smem");
-    gemm_tf32_nt_kernel<true><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, M, N, K, C, ldc,
-                                                             alpha, beta, err);
+    gemm_tf32_nt_kernel<true><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
+                                                             N, K, C, ldc, alpha, beta, err);
   } else {
     const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
     LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                   "gemm_tf32: set smem");
-    gemm_tf32_nt_kernel<false><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, M, N, K, C, ldc,
-                                                              alpha, beta, err);
+    gemm_tf32_nt_kernel<false><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
+                                                              N, K, C, ldc, alpha, beta, err);
   }
   return check_launch("gemm_tf32");
 }

@@ -261,7 +261,7 @@ class IRResult:
     x: torch.Tensor          # (k, n) solutions
     berr: list               # normwise backward error per right-hand side
     outer: int               # refinement steps
-    inner_steps: list        # GMRES outer iterations (restart cycles) per refinement step
+    inner_steps: list        # GMRES restart cycles per refinement step (0: plain refinement)
     converged: bool
     fallback: bool = False   # solved by the FP64 LU after GMRES-IR stalled
 
@@ -278,8 +278,11 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     then x += ||r||_inf d and r = b - A x, until the normwise backward error
     of every right-hand side is <= tol.  arith "df" runs the inner operator
     and preconditioner products in double-float (FP64-accurate) arithmetic,
-    "fp32" in FP32 (classic mixed-precision refinement); the outer residual is
-    always FP64-accurate (A as a 48-bit hi + lo pair, double-float sums).
+    "fp32" in FP32; "ir" replaces the GMRES solve by one preconditioner
+    product (x += M^{-1} r: classic LU iterative refinement, enough when
+    kappa(A) u_f is well below 1); "auto" starts with "ir" and moves to "df"
+    GMRES when a step stalls.  The outer residual is always FP64-accurate (A
+    as a 48-bit hi + lo pair, double-float sums).
 
     fallback=True stops refining as soon as it stalls (an inner solve that
     does not reach inner_rtol, or a refinement step that shrinks the largest
@@ -299,8 +302,15 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     if split is None:
         split = split_matrix(a64)
     outer_op = SplitMatrixOperator(split, "df")
-    inner_op = outer_op if arith == "df" else SplitMatrixOperator(split, arith)
-    pre = InverseLUPreconditioner(factor, inverse, arith)
+    tiers = ["ir", "df"] if arith == "auto" else [arith]
+    tier = 0
+
+    def inner(t):
+        kind = tiers[t]
+        op = outer_op if kind in ("df", "ir") else SplitMatrixOperator(split, kind)
+        return op, InverseLUPreconditioner(factor, inverse, "df" if kind == "ir" else kind)
+
+    inner_op, pre = inner(tier)
     anorm = float(norm_inf(a64).item())
     bnorm = _kmax(b64).cpu()
     x = torch.zeros_like(b64)
@@ -308,22 +318,32 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     st = _ffi.stream_handle(a64.device)
     inner_steps, berr, converged, it = [], [float("inf")] * k, False, 0
     for it in range(1, max_outer + 1):
-        rn = _kmax(r)
-        rhat = r.clone()
-        _ffi.call("lxgb_rows_scale_f64", k, n, _ffi.ptr(rn), 1, _ffi.ptr(rhat), st)
-        res = _krylov.gmres_block(inner_op, rhat, rtol=inner_rtol, atol=inner_rtol,
-                                  restart=restart, stagnation_iters=stagnation_iters,
-                                  max_steps=inner_max_steps, preconditioner=pre)
-        inner_steps.append(max(res.steps))
-        _ffi.call("lxgb_rows_axpy_f64", k, n, _ffi.ptr(rn), _ffi.ptr(res.y), _ffi.ptr(x), st)
+        if tiers[tier] == "ir":
+            # plain refinement: x += M^{-1} r (one preconditioner product)
+            x.add_(pre.mv_block(r))
+            inner_steps.append(0)
+            inner_ok = True
+        else:
+            rn = _kmax(r)
+            rhat = r.clone()
+            _ffi.call("lxgb_rows_scale_f64", k, n, _ffi.ptr(rn), 1, _ffi.ptr(rhat), st)
+            res = _krylov.gmres_block(inner_op, rhat, rtol=inner_rtol, atol=inner_rtol,
+                                      restart=restart, stagnation_iters=stagnation_iters,
+                                      max_steps=inner_max_steps, preconditioner=pre)
+            inner_steps.append(max(res.steps))
+            _ffi.call("lxgb_rows_axpy_f64", k, n, _ffi.ptr(rn), _ffi.ptr(res.y), _ffi.ptr(x), st)
+            inner_ok = all(code == _krylov.SUCCESSFUL for code in res.results)
         r = outer_op.residual(x, b64)
         prev = max(berr)
         berr = _berr(r, x, anorm, bnorm)
         if all(e <= tol for e in berr):
             converged = True
             break
-        stalled = any(code != _krylov.SUCCESSFUL for code in res.results) or max(berr) > prev / 2
-        if fallback and stalled:
+        stalled = not inner_ok or not (max(berr) <= prev / 2)
+        if stalled and tier + 1 < len(tiers):
+            tier += 1
+            inner_op, pre = inner(tier)
+        elif fallback and stalled:
             return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
     if fallback and not converged:
         return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)

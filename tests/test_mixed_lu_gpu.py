@@ -124,7 +124,9 @@ def test_double_float_gemv(dev, m, n, k):
 
 
 @pytest.mark.parametrize("n,cond,arith", [(256, 1e2, "df"), (512, 1e6, "df"), (1024, 1e2, "df"),
-                                          (1024, 1e6, "df"), (512, 1e2, "fp32")])
+                                          (1024, 1e6, "df"), (512, 1e2, "fp32"),
+                                          (512, 1e6, "auto"), (1024, 1e2, "auto"),
+                                          (1024, 1e2, "ir")])
 def test_gmres_ir_reaches_fp64_backward_error(dev, n, cond, arith):
     a = conditioned(n, cond, n + int(np.log10(cond)))
     rng = np.random.default_rng(7)

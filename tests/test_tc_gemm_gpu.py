@@ -55,3 +55,34 @@ def test_3xtf32_gemm_reaches_fp32_accuracy(dev, m, n, k):
     # FP32-level: sqrt(k) 2^-24 accumulation plus the dropped lo*lo term
     # (plain TF32 products give ~1e-3 here)
     assert rel < 1e-5, rel
+
+
+@pytest.mark.parametrize("layout", ["aligned", "odd_ld", "offset", "beta0"])
+def test_tf32_gemm_epilogue_layouts(dev, layout):
+    """C updated through the TMA epilogue (16-byte base and row stride) and
+    through the direct-store epilogue (any other C) gives the same values."""
+    m, n, k = 300, 200, 64
+    g = torch.Generator(device=dev).manual_seed(17)
+    a = torch.randn(m, k, device=dev, generator=g)
+    b = torch.randn(n, k, device=dev, generator=g)
+    big = torch.randn(m + 1, n + 5, device=dev, generator=g)
+    if layout == "odd_ld":
+        c = big[:m, :n]            # row stride n + 5: not a multiple of 4
+    elif layout == "offset":
+        c = big[1:, 1:n + 1]       # base 4 bytes past a 16-byte boundary
+    else:
+        c = torch.randn(m, n, device=dev, generator=g)
+    beta = 0.0 if layout == "beta0" else 1.0
+    c0 = c.clone()
+    outside = big.clone()
+    _blas.gemm_tf32_nt(a, b, c, alpha=-1.0, beta=beta)
+    r = ref(a, b, c0, -1.0, beta)
+    bound = (k * 2.0 ** -10) * float(a.abs().max() * b.abs().max()) + 1e-5
+    assert float((c.double() - r).abs().max()) <= bound
+    if layout in ("odd_ld", "offset"):   # nothing outside the C view was written
+        mask = torch.ones_like(big, dtype=torch.bool)
+        if layout == "odd_ld":
+            mask[:m, :n] = False
+        else:
+            mask[1:, 1:n + 1] = False
+        assert torch.equal(big[mask], outside[mask])
