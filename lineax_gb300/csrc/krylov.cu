@@ -22,6 +22,31 @@ __device__ __forceinline__ double nanmax2(double a, double b) {
   return (a != a || b != b) ? NAN : fmax(a, b);
 }
 
+// |v| / s compared with 1 without dividing (GB300's FP64 pipe makes a
+// division per element the most expensive part of a Krylov iteration):
+// code 0 when the quotient is <= 1, 1 when it is > 1, 2 when it is NaN
+// (v or s NaN, 0/0, inf/inf).  For finite positive s, |v| > s exactly when
+// fl(|v| / s) > 1, and non-negative doubles order like their bit patterns.
+// The max code over the elements, as the class 0.0 / 2.0 / NaN compared with
+// 1, is the lineax test  max_norm(v / s) > 1.
+__device__ __forceinline__ int ratio_code(double v, double s) {
+  const long long kInf = 0x7FF0000000000000LL;
+  const long long av = __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFLL;
+  const long long sb = __double_as_longlong(s);
+  const long long as = sb & 0x7FFFFFFFFFFFFFFFLL;
+  if (av > kInf || as > kInf) return 2;
+  if (as == 0) return av == 0 ? 2 : 1;
+  if (as == kInf) return av == kInf ? 2 : 0;
+  if (sb < 0) return 0;  // negative finite s: the quotient is <= 0
+  return av > sb ? 1 : 0;
+}
+
+// Codes 0/1/2 (integer max over elements, on the integer pipe) back to the
+// classes 0.0 / 2.0 / NaN that the FP64 max-norm combination expects.
+__device__ __forceinline__ double code_class(int code) {
+  return code == 0 ? 0.0 : (code == 1 ? 2.0 : NAN);
+}
+
 static int kparts(int64_t n) {
   int64_t p = (n + kKThreads * 4 - 1) / (kKThreads * 4);
   if (p < 1) p = 1;
@@ -102,13 +127,15 @@ cg_dot_partial_kernel(int64_t n, const double* __restrict__ x, const double* __r
   const int c = blockIdx.y;
   const double* xc = x + (int64_t)c * n;
   const double* yc = y + (int64_t)c * n;
-  double acc = 0.0, mx = 0.0;
+  double acc = 0.0;
+  int code = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double yi = yc[i];
     acc = fma(xc[i], yi, acc);
-    if (pn1) mx = nanmax2(mx, fabs(yi / (atol + rtol * fabs(bvec[(int64_t)c * n + i]))));
+    if (pn1) code = max(code, ratio_code(yi, fma(rtol, fabs(bvec[(int64_t)c * n + i]), atol)));
   }
+  const double mx = code_class(code);
   const double s = block_reduce<false>(acc, sm);
   if (threadIdx.x == 0) part[(int64_t)c * gridDim.x + blockIdx.x] = s;
   if (pn1) {
@@ -168,7 +195,7 @@ cg_update_kernel(int64_t n, int k, CgWork w, int cur, const double* __restrict__
   __shared__ double sm[kKThreads / 32];
   const int c = blockIdx.y;
   const bool act = w.act[cur * k + c] != 0;
-  double mx = 0.0;
+  int code = 0;
   if (act) {
     const double a = w.alpha[c];
     const int64_t o = (int64_t)c * n;
@@ -177,10 +204,11 @@ cg_update_kernel(int64_t n, int k, CgWork w, int cur, const double* __restrict__
       const double d = a * p[o + i];
       const double yn = y[o + i] + d;
       y[o + i] = yn;
-      mx = nanmax2(mx, fabs(d / (atol + rtol * fabs(yn))));
+      code = max(code, ratio_code(d, fma(rtol, fabs(yn), atol)));
       if (cheap_r) r[o + i] = fma(-a, mat_p[o + i], r[o + i]);
     }
   }
+  const double mx = code_class(code);
   const double m = block_reduce<true>(mx, sm);
   if (threadIdx.x == 0) w.pn2[(int64_t)c * gridDim.x + blockIdx.x] = m;
 }
@@ -243,7 +271,8 @@ __global__ void copy_vec_kernel(int64_t total, const double* __restrict__ src,
 
 // 5-point negative Laplacian on an nx×ny interior grid with Dirichlet zero
 // boundary: (A u)[i,j] = 4u[i,j] - u[i-1,j] - u[i+1,j] - u[i,j-1] - u[i,j+1],
-// scaled by `scale`; k vectors back to back.
+// scaled by `scale`; k vectors back to back.  Evaluated as
+// fma(4, u[i,j], -((u[i-1,j] + u[i+1,j]) + (u[i,j-1] + u[i,j+1]))).
 __global__ void __launch_bounds__(256)
 poisson5_kernel(int64_t nx, int64_t ny, int k, double scale, const double* __restrict__ u,
                 double* __restrict__ out) {
@@ -259,7 +288,9 @@ poisson5_kernel(int64_t nx, int64_t ny, int k, double scale, const double* __res
   const double dn = (i + 1 < nx) ? uc[o + ny] : 0.0;
   const double lf = (j > 0) ? uc[o - 1] : 0.0;
   const double rt = (j + 1 < ny) ? uc[o + 1] : 0.0;
-  out[(int64_t)c * n + o] = scale * (4.0 * cen - up - dn - lf - rt);
+  // four FP64 operations (the FP64 pipe bounds this kernel on GB300)
+  const double v = fma(4.0, cen, -((up + dn) + (lf + rt)));
+  out[(int64_t)c * n + o] = (scale == 1.0) ? v : scale * v;
 }
 
 // ---------------------------------------------------------------------------
@@ -776,8 +807,8 @@ gm_outer_partial_kernel(int64_t n, int k, GmWork w, const double* __restrict__ b
        i += (int64_t)gridDim.x * blockDim.x) {
     const double ri = r[o + i];
     m0 = nanmax2(m0, fabs(ri));
-    m1 = nanmax2(m1, fabs(ri / (atol + rtol * fabs(b[o + i]))));
-    m2 = nanmax2(m2, fabs(diff[o + i] / (atol + rtol * fabs(y[o + i]))));
+    m1 = nanmax2(m1, code_class(ratio_code(ri, fma(rtol, fabs(b[o + i]), atol))));
+    m2 = nanmax2(m2, code_class(ratio_code(diff[o + i], fma(rtol, fabs(y[o + i]), atol))));
   }
   const int R = w.R;
   double* part = w.part + (int64_t)c * w.parts * (R + 2);
