@@ -673,6 +673,61 @@ def run_cg_poisson(args):
     print(json.dumps(out), flush=True)
 
 
+def run_serve(args):
+    """Serving mix (50% LU / 30% Cholesky / 20% QR, n log-uniform [32, 4096],
+    1-16 right-hand sides, 30% on a resident operator): saturation throughput
+    of the mixed-precision server and of the plain FP64 server on the same
+    requests, then open-loop Poisson arrivals for p50/p99 latency."""
+    import torch
+
+    from lineax_gb300 import serve
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    count = args.serve_requests
+    warm = serve.synthetic_requests(24, seed=99, nmax=1024)
+
+    def pct(v, p):
+        v = sorted(v)
+        return v[min(len(v) - 1, int(round(p / 100.0 * (len(v) - 1))))]
+
+    def one(mode, rate, seed):
+        reqs = serve.synthetic_requests(count, seed=seed, nmax=args.serve_nmax, rate=rate)
+        for r in reqs:
+            if r.a is not None:
+                r.a = r.a.pin_memory()
+            r.b = r.b.pin_memory()
+        srv = serve.SolveServer(dev, mode=mode, hbm_budget=int(args.serve_budget_gb * 2**30))
+        t0 = time.perf_counter()
+        out = srv.run(reqs, realtime=True)
+        wall = time.perf_counter() - t0
+        lat = [c.latency * 1e3 for c in out]
+        return {"mode": mode, "offered_rate": rate, "requests": len(out),
+                "solves_per_s": len(out) / wall,
+                "rhs_per_s": sum(r.nrhs for r in reqs) / wall, "wall_s": wall,
+                "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                "max_berr": max(c.berr for c in out),
+                "fallbacks": sum(c.fallback for c in out),
+                "reused": sum(c.reused for c in out),
+                "routes": {k: sum(c.route == k for c in out)
+                           for k in ("chol_ragged", "lu_small", "lu_mixed", "lu_f64")}}
+
+    for mode in ("mixed", "fp64"):
+        serve.SolveServer(dev, mode=mode).run(warm, realtime=False)
+    torch.cuda.synchronize()
+    sat = {m: one(m, None, 5) for m in ("fp64", "mixed")}
+    for m in ("fp64", "mixed"):
+        print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
+                          "saturation", **sat[m]}), flush=True)
+    rate = 0.5 * sat["fp64"]["solves_per_s"]
+    for m in ("fp64", "mixed"):
+        print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
+                          "open_loop", **one(m, rate, 6)}), flush=True)
+    rate = 0.5 * sat["mixed"]["solves_per_s"]
+    print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
+                      "open_loop", **one("mixed", rate, 6)}), flush=True)
+
+
 def main():
     global COUNT
     p = argparse.ArgumentParser()
@@ -684,7 +739,8 @@ def main():
     p.add_argument("--systems", type=int, default=COUNT,
                    help="systems per GPU (smaller values are for profiling runs only)")
     p.add_argument("--workload", default="ragged_cholesky",
-                   choices=["ragged_cholesky", "gmres_ir", "lu_batch", "qr_ls", "cg_poisson"],
+                   choices=["ragged_cholesky", "gmres_ir", "lu_batch", "qr_ls", "cg_poisson",
+                            "serve"],
                    help="gmres_ir: the dense mixed-precision LU + GMRES-IR workload")
     p.add_argument("--n", type=int, default=8192, help="order for --workload gmres_ir")
     p.add_argument("--restart", type=int, default=8, help="GMRES restart for --workload gmres_ir")
@@ -697,6 +753,9 @@ def main():
     p.add_argument("--cg-rhs", type=int, default=64, help="right-hand sides (cg_poisson)")
     p.add_argument("--cg-iters", type=int, default=200, help="timed CG iterations (cg_poisson)")
     p.add_argument("--cg-full", action="store_true", help="also run CG to rtol 1e-10")
+    p.add_argument("--serve-requests", type=int, default=300, help="requests (serve)")
+    p.add_argument("--serve-nmax", type=int, default=4096, help="largest order (serve)")
+    p.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget (serve)")
     p.add_argument("--arith", default="auto", choices=["auto", "df", "fp32"],
                    help="inner GMRES arithmetic (gmres_ir)")
     p.add_argument("--precisions", default="tf32,3xtf32", help="factor precisions (gmres_ir)")
@@ -708,9 +767,9 @@ def main():
     if args.workload == "gmres_ir":
         run_gmres_ir(args)
         return
-    if args.workload in ("lu_batch", "qr_ls", "cg_poisson"):
-        {"lu_batch": run_lu_batch, "qr_ls": run_qr_ls, "cg_poisson": run_cg_poisson}[
-            args.workload](args)
+    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve"):
+        {"lu_batch": run_lu_batch, "qr_ls": run_qr_ls, "cg_poisson": run_cg_poisson,
+         "serve": run_serve}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,413 @@
+"""Continuous-batching solve server on one GPU.
+
+Requests are dense square systems A X = B (1 to 16 right-hand sides) tagged
+with the lineax solver the client asked for (LU, Cholesky or QR) and an
+operator id; a request may omit A and reuse an operator the server has seen,
+in which case a resident factor (kept in device memory under an LRU policy)
+skips the factorisation.  Each scheduling round admits the queued requests
+that have arrived, first come first served, while their device footprint
+plus the resident factors fits the HBM budget, and runs them grouped by
+route:
+
+  chol_ragged  Cholesky requests with n <= 1024: one launch of the ragged
+               mixed-precision SPD kernel (FP32 factor, FP64-accurate
+               refinement) for the whole group; systems it does not solve to
+               the tolerance are re-solved by FP64 LU.
+  lu_small     other requests with n <= 168: batched FP64 LU, one launch per
+               distinct order (each system's arithmetic is the same as alone;
+               right-hand-side blocks are zero padded, and each vector is
+               solved independently).
+  lu_mixed     the rest: FP32 LU with TF32/3xTF32 tensor-core updates, its
+               triangular inverses and GMRES-IR to FP64 backward error
+               (lineax_gb300.mixed), FP64 LU when refinement stalls; the
+               factor stays resident for later requests on the operator.
+
+mode="fp64" serves the same requests with the plain FP64 GPU path of this
+library (ragged FP64 Cholesky, FP64 LU): the denominator of the mixed
+path's speed-up.  A square QR request is served by LU in both modes: for a
+nonsingular square A both define the same solution, and lineax's own
+AutoLinearSolver picks LU for square operators (lineax/_solve.py:555-600).
+Every completion carries its normwise backward error; a request's result
+does not depend on what else was in its batch.
+"""
+
+from __future__ import annotations
+
+import collections
+import dataclasses
+import time
+
+import torch
+
+from . import _blas, _dense, _ffi, batched, mixed
+
+KINDS = ("lu", "cholesky", "qr")
+SMALL_LU_MAX = 168      # one CTA per system, matrix in shared memory
+RAGGED_CHOL_MAX = 1024  # the ragged mixed-precision Cholesky kernel's limit
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    kind: str                         # "lu", "cholesky" or "qr"
+    b: torch.Tensor                   # (nrhs, n) FP64, host or device
+    op_id: int                        # operator identity (reuse key)
+    a: torch.Tensor | None = None     # (n, n) FP64; None: the registered operator op_id
+    arrival: float = 0.0              # seconds after the start of the run
+
+    @property
+    def n(self) -> int:
+        return int(self.b.shape[-1])
+
+    @property
+    def nrhs(self) -> int:
+        return 1 if self.b.ndim == 1 else int(self.b.shape[0])
+
+
+@dataclasses.dataclass
+class Completion:
+    rid: int
+    x: torch.Tensor       # (nrhs, n) FP64 on the device
+    berr: float           # max normwise backward error over the right-hand sides
+    route: str
+    fallback: bool        # re-solved by FP64 LU
+    reused: bool          # served from a resident factor
+    finished: float = 0.0
+    latency: float = 0.0
+
+
+def route_of(kind: str, n: int, mode: str) -> str:
+    if kind not in KINDS:
+        raise ValueError(f"unknown request kind {kind!r}")
+    if kind == "cholesky" and n <= RAGGED_CHOL_MAX:
+        return "chol_ragged"
+    if n <= SMALL_LU_MAX:
+        return "lu_small"
+    return "lu_mixed" if mode == "mixed" else "lu_f64"
+
+
+def footprint(route: str, n: int, nrhs: int) -> int:
+    """Device bytes a request holds while it is being served."""
+    vec = 8 * 8 * n * max(nrhs, 1)  # b, x, residual and workspace vectors
+    if route == "chol_ragged":
+        return 8 * n * n + 4 * n * n + vec
+    if route == "lu_small":
+        return 3 * 8 * SMALL_LU_MAX * SMALL_LU_MAX + vec
+    if route == "lu_f64":
+        return 2 * 8 * n * n + vec
+    n4 = (n + 3) // 4 * 4
+    return resident_bytes(route, n) + 5 * 4 * 64 * n4 + vec
+
+
+def resident_bytes(route: str, n: int) -> int:
+    """Bytes of what stays resident for an operator between requests."""
+    if route == "lu_mixed":
+        n4 = (n + 3) // 4 * 4
+        # A (FP64), FP32 factor, both triangular inverses, A as a hi + lo pair
+        return 8 * n4 * n4 + 4 * n4 * n4 + 8 * n4 * n4 + 8 * n4 * n4
+    if route == "lu_f64":
+        return 2 * 8 * n * n  # A and its FP64 factor
+    return 8 * n * n          # the operator itself
+
+
+class Scheduler:
+    """First-come-first-served admission under a device-memory budget, with
+    an LRU cache of resident operators charged against the same budget.  Host
+    logic only: the server supplies what is resident and what it costs."""
+
+    def __init__(self, budget_bytes: int, mode: str = "mixed"):
+        self.budget = int(budget_bytes)
+        self.mode = mode
+        self.queue: collections.deque = collections.deque()
+        self.resident: collections.OrderedDict = collections.OrderedDict()
+        self.resident_total = 0
+        self.rejected: list = []
+
+    def submit(self, req: Request) -> None:
+        self.queue.append(req)
+
+    def pending(self) -> int:
+        return len(self.queue)
+
+    def next_arrival(self):
+        return self.queue[0].arrival if self.queue else None
+
+    def _evict_for(self, need: int, pinned: set) -> None:
+        for op_id in list(self.resident):
+            if self.resident_total + need <= self.budget:
+                return
+            if op_id in pinned:
+                continue
+            nbytes, _ = self.resident.pop(op_id)
+            self.resident_total -= nbytes
+
+    def admit(self, now: float) -> list:
+        """Requests that have arrived by `now`, in order, while they fit."""
+        batch, used, pinned = [], 0, set()
+        while self.queue and self.queue[0].arrival <= now:
+            req = self.queue[0]
+            route = route_of(req.kind, req.n, self.mode)
+            need = footprint(route, req.n, req.nrhs)
+            if req.op_id in self.resident:  # its resident part is already charged
+                need = max(need - self.resident[req.op_id][0], 0)
+            self._evict_for(used + need, pinned | {req.op_id})
+            if self.resident_total + used + need > self.budget:
+                if not batch and need > self.budget:
+                    self.rejected.append(self.queue.popleft())  # can never fit
+                    continue
+                break
+            batch.append(self.queue.popleft())
+            used += need
+            pinned.add(req.op_id)
+        return batch
+
+    def lookup(self, op_id):
+        hit = self.resident.get(op_id)
+        if hit is None:
+            return None
+        self.resident.move_to_end(op_id)
+        return hit[1]
+
+    def remember(self, op_id, nbytes: int, payload) -> None:
+        if op_id in self.resident:
+            self.resident_total -= self.resident.pop(op_id)[0]
+        self._evict_for(nbytes, {op_id})
+        if self.resident_total + nbytes <= self.budget:
+            self.resident[op_id] = (int(nbytes), payload)
+            self.resident_total += int(nbytes)
+
+
+def _pad_identity(a: torch.Tensor, n_to: int) -> torch.Tensor:
+    n = a.shape[0]
+    if n == n_to:
+        return a.contiguous()
+    out = torch.zeros((n_to, n_to), dtype=torch.float64, device=a.device)
+    out[:n, :n] = a
+    idx = torch.arange(n, n_to, device=a.device)
+    out[idx, idx] = 1.0
+    return out
+
+
+def _berr(a: torch.Tensor, x: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Per-vector normwise backward error (device), FP64 residual."""
+    r = _blas.gemv(a, x, alpha=-1.0, beta=1.0, out=b.clone())
+    anorm = mixed.norm_inf(a)
+    return r.abs().amax(dim=1) / (anorm * x.abs().amax(dim=1) + b.abs().amax(dim=1))
+
+
+@dataclasses.dataclass
+class _MixedOperator:
+    n: int
+    n4: int
+    a: torch.Tensor
+    factor: mixed.LU32
+    inverse: mixed.InverseLU32
+    split: mixed.SplitMatrix
+
+
+@dataclasses.dataclass
+class _F64Operator:
+    a: torch.Tensor
+    lu: torch.Tensor
+    piv: torch.Tensor
+
+
+class SolveServer:
+    """Serve Requests on one GPU (see the module docstring)."""
+
+    def __init__(self, device="cuda", mode: str = "mixed", hbm_budget: int = 64 << 30,
+                 tol: float = 1e-12, precision: str = "3xtf32"):
+        if mode not in ("mixed", "fp64"):
+            raise ValueError("mode must be 'mixed' or 'fp64'")
+        self.device = torch.device(device)
+        self.mode = mode
+        self.tol = tol
+        self.precision = precision
+        self.sched = Scheduler(hbm_budget, mode)
+        self.registry: dict = {}  # op_id -> host FP64 matrix (the client's copy)
+        self._ws = None
+
+    def register(self, op_id, a_host: torch.Tensor) -> None:
+        self.registry[op_id] = a_host
+
+    # -- execution ------------------------------------------------------------
+
+    def _matrix(self, req: Request) -> torch.Tensor:
+        a = req.a if req.a is not None else self.registry[req.op_id]
+        if req.a is not None:
+            self.registry.setdefault(req.op_id, req.a)
+        return a.to(self.device, torch.float64, non_blocking=True)
+
+    def _rhs(self, req: Request) -> torch.Tensor:
+        b = req.b.reshape(req.nrhs, req.n)
+        return b.to(self.device, torch.float64, non_blocking=True).contiguous()
+
+    def _fp64_lu(self, a: torch.Tensor, b: torch.Tensor):
+        lu, piv = _dense.lu_factor(a)
+        return _dense.lu_solve(lu, piv, b), lu, piv
+
+    def _run_chol(self, reqs: list) -> list:
+        mats = [self._matrix(r) for r in reqs]
+        rhs = [self._rhs(r) for r in reqs]
+        rb = batched.RaggedBatch.from_lists(mats, rhs, device=self.device)
+        out = []
+        if self.mode == "mixed":
+            if self._ws is None or not self._ws.fits(rb.batch, rb.max_n, rb.max_nrhs):
+                self._ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, self.device)
+            res = batched.spd_solve_ragged_mixed(rb, tol=self.tol, workspace=self._ws)
+            info = res.info.cpu().tolist()
+            berr = res.berr.cpu().tolist()
+            for s, req in enumerate(reqs):
+                x = rb.system_b(res.x, s).clone()
+                if info[s] != 0 or not berr[s] <= self.tol:
+                    x, _, _ = self._fp64_lu(mats[s], rhs[s])
+                    e = float(_berr(mats[s], x, rhs[s]).max())
+                    out.append(Completion(req.rid, x, e, "chol_ragged", True, False))
+                else:
+                    out.append(Completion(req.rid, x, berr[s], "chol_ragged", False, False))
+            return out
+        x, info = batched.cholesky_solve_ragged(rb)
+        info = info.cpu().tolist()
+        errs = []
+        xs = []
+        for s in range(len(reqs)):
+            xv = rb.system_b(x, s).clone()
+            if info[s] != 0:
+                xv, _, _ = self._fp64_lu(mats[s], rhs[s])
+            xs.append(xv)
+            errs.append(_berr(mats[s], xv, rhs[s]).max())
+        errs = torch.stack(errs).cpu().tolist() if errs else []
+        return [Completion(r.rid, xs[s], errs[s], "chol_ragged", info[s] != 0, False)
+                for s, r in enumerate(reqs)]
+
+    def _run_small(self, reqs: list) -> list:
+        mats = [self._matrix(r) for r in reqs]
+        rhs = [self._rhs(r) for r in reqs]
+        xs = [None] * len(reqs)
+        by_n = collections.defaultdict(list)
+        for s, r in enumerate(reqs):
+            by_n[r.n].append(s)
+        for n, idx in by_n.items():  # one batched launch per order
+            kmax = max(reqs[s].nrhs for s in idx)
+            a = torch.stack([mats[s] for s in idx])
+            b = torch.zeros((len(idx), kmax, n), dtype=torch.float64, device=self.device)
+            for j, s in enumerate(idx):
+                b[j, : reqs[s].nrhs] = rhs[s]
+            lu, piv, _ = _dense.lu_factor_batched(a)
+            x = _dense.lu_solve_batched(lu, piv, b)
+            for j, s in enumerate(idx):
+                xs[s] = x[j, : reqs[s].nrhs].contiguous()
+        errs = torch.stack([_berr(mats[s], xs[s], rhs[s]).max() for s in range(len(reqs))])
+        errs = errs.cpu().tolist()
+        return [Completion(r.rid, xs[s], errs[s], "lu_small", False, False)
+                for s, r in enumerate(reqs)]
+
+    def _run_mixed(self, req: Request) -> Completion:
+        op = self.sched.lookup(req.op_id)
+        reused = op is not None
+        if op is None:
+            a = self._matrix(req)
+            n4 = (req.n + 3) // 4 * 4
+            ap = _pad_identity(a, n4)
+            f = mixed.lu_factor_tf32(ap, self.precision)
+            op = _MixedOperator(req.n, n4, ap, f, mixed.lu_inverse(f, self.precision),
+                                mixed.split_matrix(ap))
+        b = self._rhs(req)
+        bp = b if op.n4 == req.n else torch.cat(
+            [b, torch.zeros((req.nrhs, op.n4 - req.n), dtype=torch.float64, device=b.device)], 1)
+        res = mixed.gmres_ir(op.a, bp, tol=self.tol, max_outer=20, inner_max_steps=5, restart=8,
+                             factor=op.factor, inverse=op.inverse, split=op.split,
+                             precision=self.precision, arith="auto", fallback=True)
+        self.sched.remember(req.op_id, resident_bytes("lu_mixed", req.n), op)
+        x = res.x[:, : req.n].contiguous()
+        return Completion(req.rid, x, max(res.berr), "lu_mixed", res.fallback, reused)
+
+    def _run_f64(self, req: Request) -> Completion:
+        op = self.sched.lookup(req.op_id)
+        reused = op is not None
+        if op is None:
+            a = self._matrix(req)
+            lu, piv = _dense.lu_factor(a)
+            op = _F64Operator(a, lu, piv)
+        b = self._rhs(req)
+        x = _dense.lu_solve(op.lu, op.piv, b)
+        self.sched.remember(req.op_id, resident_bytes("lu_f64", req.n), op)
+        return Completion(req.rid, x, float(_berr(op.a, x, b).max()), "lu_f64", False, reused)
+
+    def execute(self, batch: list) -> list:
+        """Serve one admitted batch (synchronises before returning)."""
+        groups = collections.defaultdict(list)
+        for r in batch:
+            groups[route_of(r.kind, r.n, self.mode)].append(r)
+        out = []
+        if groups["chol_ragged"]:
+            out += self._run_chol(groups["chol_ragged"])
+        if groups["lu_small"]:
+            out += self._run_small(groups["lu_small"])
+        for r in groups["lu_mixed"]:
+            out.append(self._run_mixed(r))
+        for r in groups["lu_f64"]:
+            out.append(self._run_f64(r))
+        torch.cuda.synchronize(self.device)
+        return out
+
+    def run(self, requests: list, realtime: bool = True) -> list:
+        """Serve requests whose `arrival` times are seconds after the start
+        (open loop: arrivals do not wait for completions).  Returns the
+        completions in request-id order with finish times and latencies."""
+        for r in sorted(requests, key=lambda q: q.arrival):
+            self.sched.submit(r)
+        arrival = {r.rid: r.arrival for r in requests}
+        done = {}
+        t0 = time.perf_counter()
+        while self.sched.pending():
+            now = time.perf_counter() - t0 if realtime else float("inf")
+            batch = self.sched.admit(now)
+            if not batch:
+                nxt = self.sched.next_arrival()
+                if nxt is not None and nxt > now:
+                    time.sleep(min(nxt - now, 0.01))
+                    continue
+                if not self.sched.pending():
+                    break
+                raise MemoryError("a request does not fit the HBM budget")
+            for c in self.execute(batch):
+                c.finished = time.perf_counter() - t0
+                c.latency = c.finished - arrival[c.rid]
+                done[c.rid] = c
+        return [done[k] for k in sorted(done)]
+
+
+def synthetic_requests(count: int, seed: int = 0, nmin: int = 32, nmax: int = 4096,
+                       reuse: float = 0.3, rate: float | None = None, mix=(0.5, 0.3, 0.2)):
+    """The serving mix: kinds LU/Cholesky/QR with probabilities `mix`, n
+    log-uniform on [nmin, nmax], 1-16 right-hand sides, a fraction `reuse`
+    of requests on an operator seen before (no matrix sent), Poisson arrivals
+    at `rate` per second (all at t = 0 when rate is None).  Host tensors;
+    Cholesky operators are SPD ((G + Gᵀ)/sqrt(2n) + 3I, spectrum in [1, 5]),
+    the others G/sqrt(n) + I."""
+    import numpy as np
+
+    rng = np.random.default_rng([seed, 0x5E7])
+    reqs, ops, t = [], [], 0.0
+    for rid in range(count):
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        if ops and rng.random() < reuse:
+            op_id, kind, n = ops[int(rng.integers(len(ops)))]
+            a = None
+        else:
+            kind = KINDS[int(rng.choice(3, p=list(mix)))]
+            n = int(np.clip(np.floor(np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1)))),
+                            nmin, nmax))
+            g = torch.from_numpy(rng.standard_normal((n, n)))
+            eye = torch.eye(n, dtype=torch.float64)
+            # SPD: the symmetric part scaled to spectrum [-2, 2], shifted by 3
+            a = ((g + g.T) / np.sqrt(2.0 * n) + 3.0 * eye) if kind == "cholesky" else \
+                (g / np.sqrt(n) + eye)
+            op_id = len(ops)
+            ops.append((op_id, kind, n))
+        k = int(rng.integers(1, 17))
+        b = torch.from_numpy(rng.standard_normal((k, n)))
+        reqs.append(Request(rid, kind, b, op_id, a, t))
+    return reqs

@@ -1,0 +1,89 @@
+"""Serving loop: admission and residency logic on the CPU; on the GPU, every
+request solved to FP64 backward error, results independent of the batch a
+request was served in, and resident factors reused."""
+
+import pytest
+import torch
+
+from lineax_gb300 import serve
+
+
+def req(rid, kind, n, k=1, op=None, arrival=0.0, with_a=True):
+    b = torch.zeros(k, n, dtype=torch.float64)
+    a = torch.eye(n, dtype=torch.float64) if with_a else None
+    return serve.Request(rid, kind, b, rid if op is None else op, a, arrival)
+
+
+def test_routes():
+    assert serve.route_of("cholesky", 1024, "mixed") == "chol_ragged"
+    assert serve.route_of("cholesky", 1025, "mixed") == "lu_mixed"
+    assert serve.route_of("qr", 100, "mixed") == "lu_small"
+    assert serve.route_of("lu", 169, "fp64") == "lu_f64"
+    with pytest.raises(ValueError):
+        serve.route_of("svd", 10, "mixed")
+
+
+def test_admission_is_fifo_and_respects_arrival_and_budget():
+    s = serve.Scheduler(budget_bytes=serve.footprint("lu_mixed", 2000, 1) * 2, mode="mixed")
+    for r in (req(0, "lu", 2000), req(1, "lu", 2000), req(2, "lu", 2000), req(3, "lu", 50,
+                                                                                arrival=5.0)):
+        s.submit(r)
+    first = s.admit(now=1.0)
+    assert [r.rid for r in first] == [0, 1]          # the third does not fit beside them
+    second = s.admit(now=1.0)
+    assert [r.rid for r in second] == [2]            # request 3 has not arrived yet
+    assert s.admit(now=1.0) == [] and s.next_arrival() == 5.0
+    assert [r.rid for r in s.admit(now=5.0)] == [3]
+
+
+def test_residents_are_charged_and_evicted_lru():
+    per = serve.resident_bytes("lu_mixed", 1000)
+    s = serve.Scheduler(budget_bytes=int(per * 2.5), mode="mixed")
+    s.remember("a", per, "A")
+    s.remember("b", per, "B")
+    assert s.lookup("a") == "A"                      # a becomes most recently used
+    s.remember("c", per, "C")                        # evicts b, the least recently used
+    assert s.lookup("b") is None and s.lookup("a") == "A" and s.lookup("c") == "C"
+    assert s.resident_total == 2 * per
+    # an arriving request that needs room evicts residents it does not use
+    s.submit(req(9, "lu", 1000, op="c"))
+    got = s.admit(now=0.0)
+    assert [r.rid for r in got] == [9] and s.lookup("c") == "C"
+
+
+def test_request_larger_than_budget_is_rejected():
+    s = serve.Scheduler(budget_bytes=1 << 20, mode="mixed")
+    s.submit(req(0, "lu", 4096))
+    s.submit(req(1, "lu", 40))
+    assert [r.rid for r in s.admit(now=0.0)] == [1]
+    assert [r.rid for r in s.rejected] == [0]
+
+
+def test_synthetic_mix_shapes():
+    reqs = serve.synthetic_requests(60, seed=1, nmax=600, rate=100.0)
+    assert all(r.kind in serve.KINDS and 32 <= r.n <= 600 and 1 <= r.nrhs <= 16 for r in reqs)
+    assert all(b.arrival >= a.arrival for a, b in zip(reqs, reqs[1:]))
+    reused = [r for r in reqs if r.a is None]
+    assert reused and all(any(o.op_id == r.op_id and o.a is not None for o in reqs) for r in reused)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_serve_mix_backward_error_and_batch_independence(dev, mode):
+    reqs = serve.synthetic_requests(40, seed=3, nmax=700)
+    srv = serve.SolveServer(dev, mode=mode)
+    out = srv.run(reqs, realtime=False)
+    assert len(out) == len(reqs)
+    for c, r in zip(out, reqs):
+        assert c.rid == r.rid and c.berr <= 1e-12, (c.route, c.berr)
+        assert c.x.shape == (r.nrhs, r.n)
+    assert any(c.reused for c in out) or mode == "mixed" and not any(
+        c.route == "lu_mixed" for c in out)
+    # each request again on a fresh server, alone: bit-identical results
+    for r in reqs[:12]:
+        alone = serve.SolveServer(dev, mode=mode)
+        for o in reqs:
+            if o.a is not None:
+                alone.register(o.op_id, o.a)
+        c = alone.run([serve.Request(r.rid, r.kind, r.b, r.op_id, r.a, 0.0)], realtime=False)[0]
+        assert torch.equal(c.x, out[r.rid].x), (r.kind, r.n, c.route)
