@@ -728,6 +728,59 @@ def run_serve(args):
                       "open_loop", **one("mixed", rate, 6)}), flush=True)
 
 
+def run_peaks(args):
+    """Arithmetic reference points on this GPU: library GEMMs (torch.matmul,
+    FP64 / FP32 / TF32, a sanity line) and this library's tcgen05 TF32 and
+    3xTF32 GEMM on the same square shape and on the rank-64 update shape of
+    the LU factorisations.  Best of 5 CUDA-event timings after 2 warm-ups."""
+    import torch
+
+    from lineax_gb300 import _blas
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = args.peaks_n
+    out = {"workload": f"gemm_peaks_{n}"}
+
+    def best(fn, flops):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(5):
+            e0, e1 = _events(2)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return flops / (min(ts) * 1e-3) / 1e12
+
+    g = torch.Generator(device=dev).manual_seed(0)
+    a32 = torch.randn(n, n, device=dev, generator=g)
+    b32 = torch.randn(n, n, device=dev, generator=g)
+    c32 = torch.zeros(n, n, device=dev)
+    fl = 2.0 * n ** 3
+    if not args.peaks_ours_only:
+        a64, b64 = a32.double(), b32.double()
+        out["torch_fp64_tflops"] = best(lambda: a64 @ b64, fl)
+        torch.backends.cuda.matmul.allow_tf32 = False
+        out["torch_fp32_tflops"] = best(lambda: a32 @ b32, fl)
+        torch.backends.cuda.matmul.allow_tf32 = True
+        out["torch_tf32_tflops"] = best(lambda: a32 @ b32, fl)
+        torch.backends.cuda.matmul.allow_tf32 = False
+        del a64, b64
+    out["lxgb_tf32_tflops"] = best(lambda: _blas.gemm_tf32_nt(a32, b32, c32), fl)
+    out["lxgb_3xtf32_tflops"] = best(lambda: _blas.gemm_3xtf32_nt(a32, b32, c32), fl)
+    # the LU trailing update: C (n×n) -= A (n×64) Bᵀ (n×64), C read and written
+    a_k = a32[:, :64].contiguous()
+    b_k = b32[:, :64].contiguous()
+    t = best(lambda: _blas.gemm_tf32_nt(a_k, b_k, c32, alpha=-1.0, beta=1.0), 2.0 * n * n * 64)
+    out["lxgb_tf32_rank64_tflops"] = t
+    out["lxgb_tf32_rank64_gbs"] = t * 1e12 / (2.0 * n * n * 64) * (8.0 * n * n) / 1e9
+    print(json.dumps(out), flush=True)
+
+
 def main():
     global COUNT
     p = argparse.ArgumentParser()
@@ -740,7 +793,7 @@ def main():
                    help="systems per GPU (smaller values are for profiling runs only)")
     p.add_argument("--workload", default="ragged_cholesky",
                    choices=["ragged_cholesky", "gmres_ir", "lu_batch", "qr_ls", "cg_poisson",
-                            "serve"],
+                            "serve", "peaks"],
                    help="gmres_ir: the dense mixed-precision LU + GMRES-IR workload")
     p.add_argument("--n", type=int, default=8192, help="order for --workload gmres_ir")
     p.add_argument("--restart", type=int, default=8, help="GMRES restart for --workload gmres_ir")
@@ -754,6 +807,9 @@ def main():
     p.add_argument("--cg-iters", type=int, default=200, help="timed CG iterations (cg_poisson)")
     p.add_argument("--cg-full", action="store_true", help="also run CG to rtol 1e-10")
     p.add_argument("--serve-requests", type=int, default=300, help="requests (serve)")
+    p.add_argument("--peaks-n", type=int, default=8192, help="GEMM order (peaks)")
+    p.add_argument("--peaks-ours-only", action="store_true",
+                   help="time only this library's GEMMs (peaks)")
     p.add_argument("--serve-nmax", type=int, default=4096, help="largest order (serve)")
     p.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget (serve)")
     p.add_argument("--arith", default="auto", choices=["auto", "df", "fp32"],
@@ -767,9 +823,9 @@ def main():
     if args.workload == "gmres_ir":
         run_gmres_ir(args)
         return
-    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve"):
+    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve", "peaks"):
         {"lu_batch": run_lu_batch, "qr_ls": run_qr_ls, "cg_poisson": run_cg_poisson,
-         "serve": run_serve}[args.workload](args)
+         "serve": run_serve, "peaks": run_peaks}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)
