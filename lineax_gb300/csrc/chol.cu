@@ -878,8 +878,7 @@ static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs
   float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + kQueueHeader);
   reset_queue_kernel<<<1, 1, 0, st>>>(queue);
   const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(posv_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem),
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(posv_mixed_kernel), (int)smem),
                 "posv_mixed: set smem");
   posv_mixed_kernel<<<(unsigned)grid, kMxThreads, smem, st>>>(
       batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
@@ -901,8 +900,7 @@ extern "C" int lxgb_potrf_ragged_f64(int64_t batch, int32_t max_n, const int32_t
   cudaStream_t st = as_stream(stream);
   const int ns = max_n < kCholSmemMaxF64 ? max_n : kCholSmemMaxF64;
   const size_t smem = (size_t)ns * (ns | 1) * sizeof(double);
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(potrf_ragged_f64_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(potrf_ragged_f64_kernel), (int)smem),
                 "potrf: set smem");
   const int64_t g = sm_count();
   potrf_ragged_f64_kernel<<<(unsigned)(batch < g ? batch : g), kCholThreads, smem, st>>>(
@@ -918,8 +916,7 @@ extern "C" int lxgb_potrs_ragged_f64(int64_t batch, int32_t max_n, const int32_t
   LXGB_REQUIRE(n && nrhs && a_off && u && b_off && b, "potrs: null pointer");
   const size_t smem = (size_t)max_n * sizeof(double);
   LXGB_REQUIRE(smem <= 160 * 1024, "potrs: max_n too large for the shared-memory vector");
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(potrs_ragged_f64_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(potrs_ragged_f64_kernel), (int)smem),
                 "potrs: set smem");
   const int64_t g = 4 * (int64_t)sm_count();
   potrs_ragged_f64_kernel<<<(unsigned)(batch < g ? batch : g), kCholThreads, smem,

@@ -49,6 +49,12 @@ inline int invalid(const char* fmt_msg) {
 // Number of SMs of the current device (cached per process for device 0..15).
 int sm_count();
 
+// Raises kernel `fn`'s dynamic shared-memory limit to `bytes` on the current
+// device.  The attribute persists in the context, so the driver is called only
+// the first time a kernel needs more than it was last given (repeated driver
+// calls cost microseconds of host time per launch).  Defined in status.cu.
+cudaError_t ensure_dynamic_smem(const void* fn, int bytes);
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -66,33 +66,59 @@ template <bool LOWER>
 __global__ void __launch_bounds__(kInvCols)
 inv_diag_kernel(int n, int j0, int nb, const float* __restrict__ lu, float* __restrict__ w,
                 int c_begin, int c_end, float* __restrict__ xt) {
-  __shared__ float T[kInvNB][kInvNB + 1];
+  // Tt[k][i] = T[i][k]: for a fixed k the multipliers of all rows i are
+  // contiguous (16-byte broadcast loads).  Padding rows/columns past nb hold
+  // the identity, so the fully unrolled substitution needs no bounds.
+  __shared__ __align__(16) float Tt[kInvNB][kInvNB];
   __shared__ float X[kInvNB][kInvCols + 1];
   for (int e = threadIdx.x; e < kInvNB * kInvNB; e += blockDim.x) {
     const int i = e / kInvNB, k = e % kInvNB;
-    T[i][k] = (i < nb && k < nb) ? lu[(int64_t)(j0 + i) * n + j0 + k] : 0.0f;
+    Tt[k][i] = (i < nb && k < nb) ? lu[(int64_t)(j0 + i) * n + j0 + k] : (i == k ? 1.0f : 0.0f);
   }
   const int t = threadIdx.x;
   const int cbase = c_begin + blockIdx.x * kInvCols;
   const int c = cbase + t;
+  // Each thread substitutes its own column, held in registers.
+  float x[kInvNB];
+#pragma unroll
   for (int i = 0; i < kInvNB; ++i)
-    X[i][t] = (i < nb && c < c_end) ? w[(int64_t)(j0 + i) * n + c] : 0.0f;
+    x[i] = (i < nb && c < c_end) ? w[(int64_t)(j0 + i) * n + c] : 0.0f;
   __syncthreads();
-  // Each thread substitutes its own column.
   if (LOWER) {
-    for (int k = 0; k < nb; ++k) {
-      const float xk = X[k][t];
-      for (int i = k + 1; i < nb; ++i) X[i][t] = fmaf(-T[i][k], xk, X[i][t]);
+#pragma unroll
+    for (int k = 0; k < kInvNB; ++k) {
+      const float xk = x[k];
+#pragma unroll
+      for (int i4 = (k + 1) / 4; i4 < kInvNB / 4; ++i4) {
+        const float4 tq = *reinterpret_cast<const float4*>(&Tt[k][4 * i4]);
+        if (4 * i4 + 0 > k) x[4 * i4 + 0] = fmaf(-tq.x, xk, x[4 * i4 + 0]);
+        if (4 * i4 + 1 > k) x[4 * i4 + 1] = fmaf(-tq.y, xk, x[4 * i4 + 1]);
+        if (4 * i4 + 2 > k) x[4 * i4 + 2] = fmaf(-tq.z, xk, x[4 * i4 + 2]);
+        if (4 * i4 + 3 > k) x[4 * i4 + 3] = fmaf(-tq.w, xk, x[4 * i4 + 3]);
+      }
     }
   } else {
-    for (int k = nb - 1; k >= 0; --k) {
-      const float xk = X[k][t] / T[k][k];
-      X[k][t] = xk;
-      for (int i = 0; i < k; ++i) X[i][t] = fmaf(-T[i][k], xk, X[i][t]);
+#pragma unroll
+    for (int k = kInvNB - 1; k >= 0; --k) {
+      const float xk = x[k] / Tt[k][k];
+      x[k] = xk;
+#pragma unroll
+      for (int i4 = 0; i4 < (k + 3) / 4; ++i4) {
+        const float4 tq = *reinterpret_cast<const float4*>(&Tt[k][4 * i4]);
+        if (4 * i4 + 0 < k) x[4 * i4 + 0] = fmaf(-tq.x, xk, x[4 * i4 + 0]);
+        if (4 * i4 + 1 < k) x[4 * i4 + 1] = fmaf(-tq.y, xk, x[4 * i4 + 1]);
+        if (4 * i4 + 2 < k) x[4 * i4 + 2] = fmaf(-tq.z, xk, x[4 * i4 + 2]);
+        if (4 * i4 + 3 < k) x[4 * i4 + 3] = fmaf(-tq.w, xk, x[4 * i4 + 3]);
+      }
     }
   }
-  if (c < c_end)
-    for (int i = 0; i < nb; ++i) w[(int64_t)(j0 + i) * n + c] = X[i][t];
+  if (c < c_end) {
+#pragma unroll
+    for (int i = 0; i < kInvNB; ++i)
+      if (i < nb) w[(int64_t)(j0 + i) * n + c] = x[i];
+  }
+#pragma unroll
+  for (int i = 0; i < kInvNB; ++i) X[i][t] = x[i];
   __syncthreads();
   // Transposed copy, coalesced along the 64 entries of each column.
   const int ncols = min(kInvCols, c_end - cbase);
@@ -324,8 +350,7 @@ extern "C" int lxgb_lu32_inverse(int32_t n, const float* lu, const int32_t* piv,
   }
   cudaStream_t st = as_stream(stream);
   const size_t psmem = (size_t)2 * n * sizeof(int32_t);
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(perm_from_swaps_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem),
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(perm_from_swaps_kernel), (int)psmem),
                 "lu32_inverse: set smem");
   perm_from_swaps_kernel<<<1, 1024, psmem, st>>>(n, piv, perm);
   const unsigned idg = (unsigned)(n < 4096 ? n : 4096);

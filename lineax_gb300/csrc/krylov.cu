@@ -946,8 +946,7 @@ extern "C" int lxgb_gmres_cycle_end(int32_t k, int64_t n, int32_t restart, int32
   const int cur = parity & 1;
   if (!first) {
     const size_t smem = (size_t)(restart + 1) * (restart + 2) * sizeof(double);
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(gm_lstsq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gm_lstsq_kernel), (int)smem),
                   "gmres: set smem");
     gm_lstsq_kernel<<<k, 64, smem, st>>>(k, w, cur);
   }

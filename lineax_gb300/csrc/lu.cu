@@ -373,8 +373,7 @@ extern "C" int lxgb_getrf_batched_f64(int64_t batch, int32_t n, double* a, int64
   cudaStream_t st = as_stream(stream);
   if (n <= kSmallMax) {
     const size_t smem = (size_t)n * (n | 1) * sizeof(double);
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(getrf_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(getrf_small_kernel), (int)smem),
                   "getrf: set smem");
     for (int64_t off = 0; off < batch; off += 65535LL * 1024) {
       const int64_t cnt = (batch - off < 65535LL * 1024) ? batch - off : 65535LL * 1024;
@@ -404,8 +403,7 @@ extern "C" int lxgb_getrs_batched_f64(int64_t batch, int32_t n, int32_t nrhs, co
   const int in_smem = need <= 160 * 1024;
   const size_t smem = in_smem ? need : 0;
   if (in_smem)
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(getrs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(getrs_kernel), (int)smem),
                   "getrs: set smem");
   getrs_kernel<<<(unsigned)(batch * nrhs), kSolveThreads, smem, as_stream(stream)>>>(
       n, nrhs, lu, stride_a, piv, stride_piv, b, stride_b, trans, in_smem);

@@ -3,12 +3,15 @@
 // FP32 solve used as the preconditioner of FP64 GMRES-IR.
 //
 // Right-looking blocked LU with 64-column panels:
-//   panel_getf2_cluster_kernel — getf2 on the panel held in the shared memory
-//                            of a thread-block cluster (up to 16 CTAs); the
-//                            pivot search is exchanged through distributed
-//                            shared memory.  panel_getf2_f32_kernel (one
-//                            CTA, panel in global memory) covers panels too
-//                            tall for the cluster.
+//   panel_getf2_cluster_reg_kernel — getf2 on the panel with each row in
+//                            one thread's registers across a thread-block
+//                            cluster (up to 16 CTAs × 512 rows); pivot
+//                            search and pivot row exchanged through
+//                            distributed shared memory.
+//   panel_getf2_cluster_kernel — the same with the panel in the cluster's
+//                            shared memory (taller panels); and
+//                            panel_getf2_f32_kernel (one CTA, panel in global
+//                            memory) for panels too tall for either.
 //   laswp_f32_kernel       — the panel's row interchanges on the other columns
 //   launch_inv_diag_lower  — U12 = L11^{-1} A12 in place, and U12ᵀ into a
 //                            K-major buffer for the GEMM (ir.cu)
@@ -16,6 +19,10 @@
 #include <cooperative_groups.h>
 #include <float.h>
 #include <limits.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "common.cuh"
 #include "tc_gemm.cuh"
@@ -212,6 +219,155 @@ panel_getf2_cluster_kernel(int n, int j0, int nb, int rows_per_cta, float* __res
   }
 }
 
+// The same panel factorisation with every panel row held in the registers
+// of one thread (a CTA owns up to 512 rows, a cluster up to 16 CTAs): the
+// rank-1 update of a column is 63 independent FMAs per thread instead of a
+// loop over shared memory.  Per column each CTA publishes, in a slot
+// double-buffered by column parity, its first max |a| together with that
+// row (and row kk, from its owner); after the column's single cluster
+// barrier every CTA reduces the candidates in the same order, copies the
+// winning row through distributed shared memory, and the owner of the pivot
+// row takes row kk.  The global first max is also its CTA's first max, so the
+// published row is the pivot row.  Same arithmetic and pivot choice (first
+// row of max |a|, NaN never chosen) as the shared-memory kernels.
+constexpr int kRegPanelThreads = 512;
+
+// CLUSTER = false: a one-CTA panel (m <= 512) without the cluster barrier's
+// cluster-scope release/acquire; the exchange slots are then local.
+template <bool CLUSTER>
+__global__ void __launch_bounds__(kRegPanelThreads, 1)
+panel_getf2_cluster_reg_kernel(int n, int j0, int nb, int rows_per_cta, float* __restrict__ a,
+                               int32_t* __restrict__ piv, int32_t* __restrict__ info) {
+  __shared__ float cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ __align__(16) float xbuf[2][2][kLu32NB];  // [parity][pivot row, row kk]
+  __shared__ __align__(16) float rowp[kLu32NB];
+  __shared__ float s_wv[kRegPanelThreads / 32];
+  __shared__ int s_wi[kRegPanelThreads / 32];
+  __shared__ int s_p;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ncta = CLUSTER ? (int)cluster.num_blocks() : 1;
+  const int rank = CLUSTER ? (int)cluster.block_rank() : 0;
+  // shared memory of CTA `rk` of the cluster (this CTA's own without one)
+  auto remote = [&](auto* ptr, int rk) { return CLUSTER ? cluster.map_shared_rank(ptr, rk) : ptr; };
+  const int m = n - j0;
+  const int R = rows_per_cta;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gi = rank * R + tid;  // panel row held by this thread
+  const bool has_row = tid < R && gi < m;
+  float r[kLu32NB];
+  if (has_row) {
+    const float* src = a + (int64_t)(j0 + gi) * n + j0;
+    if (nb == kLu32NB) {
+#pragma unroll
+      for (int q = 0; q < kLu32NB / 4; ++q) {
+        const float4 v = reinterpret_cast<const float4*>(src)[q];
+        r[4 * q] = v.x;
+        r[4 * q + 1] = v.y;
+        r[4 * q + 2] = v.z;
+        r[4 * q + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kLu32NB; ++j) r[j] = (j < nb) ? src[j] : 0.0f;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kLu32NB; ++j) r[j] = 0.0f;
+  }
+#pragma unroll
+  for (int kk = 0; kk < kLu32NB; ++kk) {
+    if (kk < nb) {  // uniform over the cluster
+      const int par = kk & 1;
+      // this CTA's first max |a| in column kk, and its row published with it
+      float v = -1.0f;
+      int idx = INT_MAX;
+      if (has_row && gi >= kk) {
+        const float x = fabsf(r[kk]);
+        if (x > v) { v = x; idx = gi; }
+      }
+      warp_argmax_first_f(v, idx);
+      if (lane == 0) { s_wv[warp] = v; s_wi[warp] = idx; }
+      __syncthreads();
+      if (warp == 0) {
+        v = lane < kRegPanelThreads / 32 ? s_wv[lane] : -1.0f;
+        idx = lane < kRegPanelThreads / 32 ? s_wi[lane] : INT_MAX;
+        warp_argmax_first_f(v, idx);
+        if (lane == 0) { cand_v[par] = v; cand_i[par] = idx; }
+      }
+      __syncthreads();
+      if (has_row && gi == cand_i[par]) {
+#pragma unroll
+        for (int j = 0; j < kLu32NB; ++j) xbuf[par][0][j] = r[j];
+      }
+      if (has_row && gi == kk) {
+#pragma unroll
+        for (int j = 0; j < kLu32NB; ++j) xbuf[par][1][j] = r[j];
+      }
+      if (CLUSTER) {
+        cluster.sync();  // the one cluster barrier of this column
+      } else {
+        __syncthreads();
+      }
+      if (warp == 0) {
+        float cv = -1.0f;
+        int ci = INT_MAX;
+        if (lane < ncta) {
+          cv = *remote(&cand_v[par], lane);
+          ci = *remote(&cand_i[par], lane);
+        }
+        warp_argmax_first_f(cv, ci);
+        if (lane == 0) s_p = ci;  // INT_MAX: no candidate (all NaN), keep row kk
+      }
+      __syncthreads();
+      const bool none = s_p == INT_MAX;
+      const int p = none ? kk : s_p;
+      const int own_p = p / R, own_k = kk / R;
+      // pivot row: the winning CTA's published row (row kk itself when none)
+      if (tid < kLu32NB)
+        rowp[tid] = remote(&xbuf[par][none ? 1 : 0][0], none ? own_k : own_p)[tid];
+      __syncthreads();
+      const float akk = rowp[kk];
+      if (akk != 0.0f && p != kk) {
+        if (has_row && gi == kk) {
+#pragma unroll
+          for (int j = 0; j < kLu32NB; ++j) r[j] = rowp[j];
+        } else if (has_row && gi == p) {
+          const float* rk = remote(&xbuf[par][1][0], own_k);
+#pragma unroll
+          for (int j = 0; j < kLu32NB; ++j) r[j] = rk[j];
+        }
+      }
+      if (rank == 0 && tid == 0) {
+        piv[j0 + kk] = j0 + p;
+        if (akk == 0.0f && *info == 0) *info = j0 + kk + 1;
+      }
+      if (has_row && gi > kk) {
+        float l = r[kk];
+        if (akk != 0.0f) {
+          l *= 1.0f / akk;
+          r[kk] = l;
+        }
+#pragma unroll
+        for (int j = kk + 1; j < kLu32NB; ++j) r[j] = fmaf(-l, rowp[j], r[j]);
+      }
+    }
+  }
+  if (has_row) {
+    float* dst = a + (int64_t)(j0 + gi) * n + j0;
+    if (nb == kLu32NB) {
+#pragma unroll
+      for (int q = 0; q < kLu32NB / 4; ++q)
+        reinterpret_cast<float4*>(dst)[q] =
+            make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kLu32NB; ++j)
+        if (j < nb) dst[j] = r[j];
+    }
+  }
+}
+
 // Cluster geometry for an m-row panel: 0 when it does not fit (or the device
 // cannot co-schedule the cluster), else the CTA count (rows_per_cta set).
 static int panel_cluster_size(int m, int* rows_per_cta) {
@@ -223,19 +379,118 @@ static int panel_cluster_size(int m, int* rows_per_cta) {
   return c;
 }
 
+// Whether a cluster of c CTAs with `smem` bytes each can be co-scheduled on the
+// current device (cached: the attribute and occupancy queries cost host time
+// on every panel otherwise).
+static bool panel_cluster_fits(int c, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, size_t>, bool> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(dev, c, smem);
+  auto it = known.find(key);
+  if (it != known.end()) return it->second;
+  bool ok = cudaFuncSetAttribute(panel_getf2_cluster_kernel,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            ensure_dynamic_smem(reinterpret_cast<const void*>(panel_getf2_cluster_kernel),
+                                (int)smem) == cudaSuccess;
+  if (ok) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)c);
+    cfg.blockDim = dim3(kPanelCluThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, panel_getf2_cluster_kernel, &cfg) ==
+             cudaSuccess &&
+         nclusters >= 1;
+  }
+  if (!ok) cudaGetLastError();
+  known[key] = ok;
+  return ok;
+}
+
+static bool reg_cluster_fits(int c) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, bool> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(dev, c);
+  auto it = known.find(key);
+  if (it != known.end()) return it->second;
+  bool ok = cudaFuncSetAttribute(panel_getf2_cluster_reg_kernel<true>,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (ok) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)c);
+    cfg.blockDim = dim3(kRegPanelThreads);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, panel_getf2_cluster_reg_kernel<true>, &cfg) ==
+             cudaSuccess &&
+         nclusters >= 1;
+  }
+  if (!ok) cudaGetLastError();
+  known[key] = ok;
+  return ok;
+}
+
+// Register-resident panel when every row fits one thread of a <=16-CTA
+// cluster; 0 on launch, -1 when the caller must use another kernel.
+static int launch_panel_cluster_reg(int n, int j0, int nb, float* a, int32_t* piv, int32_t* info,
+                                    cudaStream_t st) {
+  const int m = n - j0;
+  int c = (m + kRegPanelThreads - 1) / kRegPanelThreads;
+  if (c < 1) c = 1;
+  if (c > kPanelCluMax) return -1;
+  const int r = (m + c - 1) / c;
+  if (c == 1) {
+    panel_getf2_cluster_reg_kernel<false><<<1, kRegPanelThreads, 0, st>>>(n, j0, nb, r, a, piv,
+                                                                          info);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
+  if (!reg_cluster_fits(c)) return -1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c);
+  cfg.blockDim = dim3(kRegPanelThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)c;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, panel_getf2_cluster_reg_kernel<true>, n, j0, nb, r, a, piv, info) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return 0;
+}
+
 static int launch_panel_cluster(int n, int j0, int nb, float* a, int32_t* piv, int32_t* info,
                                 cudaStream_t st) {
+  if (launch_panel_cluster_reg(n, j0, nb, a, piv, info, st) == 0) return 0;
   int r = 0;
   const int c = panel_cluster_size(n - j0, &r);
   if (c == 0) return -1;
   const size_t smem = (size_t)r * kPanelLd * sizeof(float);
-  if (cudaFuncSetAttribute(panel_getf2_cluster_kernel,
-                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-      cudaFuncSetAttribute(panel_getf2_cluster_kernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-    cudaGetLastError();
-    return -1;
-  }
+  if (!panel_cluster_fits(c, smem)) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c);
   cfg.blockDim = dim3(kPanelCluThreads);
@@ -248,12 +503,6 @@ static int launch_panel_cluster(int n, int j0, int nb, float* a, int32_t* piv, i
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  int nclusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&nclusters, panel_getf2_cluster_kernel, &cfg) != cudaSuccess ||
-      nclusters < 1) {
-    cudaGetLastError();
-    return -1;
-  }
   if (cudaLaunchKernelEx(&cfg, panel_getf2_cluster_kernel, n, j0, nb, r, a, piv, info) !=
       cudaSuccess) {
     cudaGetLastError();
@@ -387,8 +636,7 @@ extern "C" int lxgb_getrs_f32(int32_t n, int32_t nrhs, const float* lu, const in
   LXGB_REQUIRE(lu && piv && b && x, "getrs_f32: null pointer");
   const size_t smem = (size_t)n * sizeof(float);
   LXGB_REQUIRE(smem <= 180 * 1024, "getrs_f32: n too large for the shared-memory vector");
-  LXGB_CUDA_TRY(cudaFuncSetAttribute(getrs_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem),
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(getrs_f32_kernel), (int)smem),
                 "getrs_f32: set smem");
   getrs_f32_kernel<<<(unsigned)nrhs, 256, smem, as_stream(stream)>>>(n, lu, piv, b, x);
   return check_launch("getrs_f32");

@@ -2,6 +2,10 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "common.cuh"
 
 namespace lxgb {
@@ -26,6 +30,20 @@ int sm_count() {
     sms = 152;
   if (dev < 16) cached[dev] = sms;
   return sms;
+}
+
+cudaError_t ensure_dynamic_smem(const void* fn, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> given;  // (kernel, device) -> bytes
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  int& have = given[{fn, dev}];
+  if (have >= bytes) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
 }
 
 }  // namespace lxgb

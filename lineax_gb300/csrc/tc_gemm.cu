@@ -400,15 +400,13 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
   dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
   if (split) {
     const size_t smem = sizeof(TcSmem<kTcStagesSplit, true>) + 1024;
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<true>), (int)smem),
                   "gemm_tf32: set smem");
     gemm_tf32_nt_kernel<true><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
                                                              N, K, C, ldc, alpha, beta, err);
   } else {
     const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tf32_nt_kernel<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<false>), (int)smem),
                   "gemm_tf32: set smem");
     gemm_tf32_nt_kernel<false><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
                                                               N, K, C, ldc, alpha, beta, err);

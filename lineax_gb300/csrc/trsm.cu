@@ -37,8 +37,7 @@ extern "C" int lxgb_trsm_f64(int32_t n, int32_t nrhs, const double* t, int64_t l
   const int in_smem = need <= 160 * 1024;
   const size_t smem = in_smem ? need : 0;
   if (in_smem)
-    LXGB_CUDA_TRY(cudaFuncSetAttribute(trsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(trsm_kernel), (int)smem),
                   "trsm: set smem");
   trsm_kernel<<<(unsigned)nrhs, kTrsmThreads, smem, as_stream(stream)>>>(
       n, t, ldt, lower, trans, unit_diag, b, in_smem);

@@ -264,6 +264,7 @@ class IRResult:
     inner_steps: list        # GMRES restart cycles per refinement step (0: plain refinement)
     converged: bool
     fallback: bool = False   # solved by the FP64 LU after GMRES-IR stalled
+    inverse: InverseLU32 | None = None  # the triangular inverses, when they were formed
 
 
 def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol: float = 1e-6,
@@ -281,7 +282,10 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     "fp32" in FP32; "ir" replaces the GMRES solve by one preconditioner
     product (x += M^{-1} r: classic LU iterative refinement, enough when
     kappa(A) u_f is well below 1); "auto" starts with "ir" and moves to "df"
-    GMRES when a step stalls.  The outer residual is always FP64-accurate (A
+    GMRES when a step stalls.  The triangular inverses are formed here when
+    `inverse` is not given: the preconditioner is applied through them
+    (one-CTA-per-vector triangular solves stream the whole factor through a
+    single SM and cost far more at these sizes).  The outer residual is always FP64-accurate (A
     as a 48-bit hi + lo pair, double-float sums).
 
     fallback=True stops refining as soon as it stalls (an inner solve that
@@ -297,18 +301,19 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     k, n = b64.shape
     if factor is None:
         factor = lu_factor_tf32(a64, precision)
-    if inverse is None:
-        inverse = lu_inverse(factor, precision)
     if split is None:
         split = split_matrix(a64)
     outer_op = SplitMatrixOperator(split, "df")
     tiers = ["ir", "df"] if arith == "auto" else [arith]
     tier = 0
+    made = {"inverse": inverse}
 
     def inner(t):
         kind = tiers[t]
+        if made["inverse"] is None:
+            made["inverse"] = lu_inverse(factor, precision)
         op = outer_op if kind in ("df", "ir") else SplitMatrixOperator(split, kind)
-        return op, InverseLUPreconditioner(factor, inverse, "df" if kind == "ir" else kind)
+        return op, InverseLUPreconditioner(factor, made["inverse"], "df" if kind == "ir" else kind)
 
     inner_op, pre = inner(tier)
     anorm = float(norm_inf(a64).item())
@@ -347,7 +352,7 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
             return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
     if fallback and not converged:
         return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
-    return IRResult(x, berr, it, inner_steps, converged)
+    return IRResult(x, berr, it, inner_steps, converged, inverse=made["inverse"])
 
 
 def _berr(r, x, anorm, bnorm) -> list:

@@ -18,9 +18,10 @@ route:
                right-hand-side blocks are zero padded, and each vector is
                solved independently).
   lu_mixed     the rest: FP32 LU with TF32/3xTF32 tensor-core updates, its
-               triangular inverses and GMRES-IR to FP64 backward error
-               (lineax_gb300.mixed), FP64 LU when refinement stalls; the
-               factor stays resident for later requests on the operator.
+               triangular inverses, and refinement to FP64 backward error
+               (lineax_gb300.mixed: plain refinement, then GMRES-IR, then FP64
+               LU when refinement stalls); the factor stays resident for later
+               requests on the operator.
 
 mode="fp64" serves the same requests with the plain FP64 GPU path of this
 library (ragged FP64 Cholesky, FP64 LU): the denominator of the mixed

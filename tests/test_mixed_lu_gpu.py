@@ -138,7 +138,8 @@ def test_gmres_ir_reaches_fp64_backward_error(dev, n, cond, arith):
     for c in range(4):
         assert res.berr[c] <= 1e-12
         assert dense.backward_error(a, x[c], b[c]) <= 1e-12
-        assert dense.forward_error(x[c], dense.lu_linear_solve(a, b[c])) <= cond * 1e-13
+        # a backward error <= 1e-12 implies a forward error <= ~2 cond * 1e-12
+        assert dense.forward_error(x[c], dense.lu_linear_solve(a, b[c])) <= 2 * cond * 1e-12
 
 
 def test_gmres_ir_falls_back_to_fp64_when_it_stalls(dev):
