@@ -9,13 +9,21 @@
 //
 // Blocked right-looking with compact-WY panels of kQrNB reflectors
 // (H_j0 ... H_{j0+nb-1} = I - V T Vᵀ, T upper triangular):
-//   qr_panel_kernel   — the reflectors of one panel (LAPACK geqr2/larfg rules)
-//   qr_larft_kernel   — T of the panel (larft, forward column-wise)
+//   qr_panel_cluster_kernel — the reflectors of one panel and its T, rows
+//                       split over a thread-block cluster (up to 16 CTAs)
+//                       whose reductions meet in distributed shared memory;
+//   qr_panel_kernel / qr_larft_kernel — the same on one CTA (fallback when a
+//                       cluster cannot be scheduled)
 //   qr_w_kernel       — W = Vᵀ C for the trailing columns C (split over rows)
 //   qr_wt_kernel      — W' = Tᵀ W (summing the splits in fixed order)
 //   qr_update_kernel  — C -= V W'  (64×64 tiles, K = nb)
 // T of every panel is kept so that ormqr applies whole panels at once.
+#include <cooperative_groups.h>
 #include <math.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 
@@ -107,6 +115,238 @@ qr_panel_kernel(int64_t mm, int nn, int j0, int pe, double* __restrict__ h,
     }
     __syncthreads();
   }
+}
+
+namespace cg = cooperative_groups;
+constexpr int kQrCluThreads = 512;
+constexpr int kQrCluMax = 16;
+
+// Block-wide sums of NV values per thread, written to out[0..NV) (thread 0's
+// view is complete after the trailing barrier).  red: [warps][NV].
+template <int NV>
+__device__ void block_sums(double (&v)[NV], double (*red)[kQrNB], double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const double s = warp_sum(v[q]);
+    if (lane == 0) red[warp][q] = s;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < NV; q += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[w][q];
+    out[q] = t;
+  }
+  __syncthreads();
+}
+
+// Reflectors of panel rows [j0, pe) of h and the panel's T, with the
+// reflector rows i in [j0, mm) split over the cluster's CTAs (rows_per_cta
+// each).  Per column k: partial sums of squares -> barrier -> every CTA forms
+// the same beta/tau/scale from the partials summed in rank order (alpha comes
+// from the owner of row k's shared memory, since the owner overwrites it) ->
+// scale the CTA's part of v_k and form partial dots v_kᵀ a_q, the owner of row
+// k adding a_q[k] (v_k[k] = 1) -> barrier -> update a_q -= tau w_q v_k.
+// Partials are double-buffered by column parity: two barriers per column.
+// Then G = VᵀV from per-CTA partials and T by larft's recurrence in CTA 0.
+// Same rules as qr_panel_kernel + qr_larft_kernel (LAPACK geqr2/larfg/larft).
+__global__ void __launch_bounds__(kQrCluThreads, 1)
+qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
+                        double* __restrict__ h, double* __restrict__ tau,
+                        double* __restrict__ t_out) {
+  __shared__ double red[kQrCluThreads / 32][kQrNB];
+  __shared__ double p_ss[2], p_alpha[2];
+  __shared__ double p_w[2][kQrNB];
+  __shared__ double G[kQrNB][kQrNB + 1];
+  __shared__ double T[kQrNB][kQrNB + 1];
+  __shared__ double s_tau, s_scal;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ncta = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int nb = pe - j0;
+  const int64_t r_lo = j0 + (int64_t)rank * rows_per_cta;
+  const int64_t r_hi = min(mm, r_lo + rows_per_cta);
+  for (int k = j0; k < pe; ++k) {
+    const int par = (k - j0) & 1;
+    double* hk = h + (int64_t)k * mm;
+    const bool own_k = (k >= r_lo && k < r_hi);
+    double ss[1] = {0.0};
+    for (int64_t i = max((int64_t)k + 1, r_lo) + tid; i < r_hi; i += blockDim.x)
+      ss[0] = fma(hk[i], hk[i], ss[0]);
+    block_sums<1>(ss, red, &p_ss[par]);
+    if (tid == 0 && own_k) p_alpha[par] = hk[k];
+    cluster.sync();
+    if (tid == 0) {
+      double xnorm2 = 0.0;
+      for (int c = 0; c < ncta; ++c) xnorm2 += *cluster.map_shared_rank(&p_ss[par], c);
+      const int own = (int)((k - j0) / rows_per_cta);
+      const double alpha = *cluster.map_shared_rank(&p_alpha[par], own);
+      const double xnorm = sqrt(xnorm2);
+      if (xnorm == 0.0) {
+        s_tau = 0.0;
+        s_scal = 1.0;
+      } else {
+        const double beta = -copysign(hypot(alpha, xnorm), alpha);
+        s_tau = (beta - alpha) / beta;
+        s_scal = 1.0 / (alpha - beta);
+        if (own_k) hk[k] = beta;
+      }
+      if (rank == 0) tau[k] = s_tau;
+    }
+    __syncthreads();
+    const double tk = s_tau;
+    const int nrem = pe - k - 1;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int64_t i_lo = max((int64_t)k + 1, r_lo);
+    if (tk != 0.0) {
+      const double sc = s_scal;
+      for (int64_t i = i_lo + tid; i < r_hi; i += blockDim.x) hk[i] *= sc;
+    }
+    __syncthreads();
+    // one warp per trailing column: w_q partial = v_kᵀ a_q over this CTA's
+    // rows (+ a_q[k] from the owner of row k, as v_k[k] = 1)
+    for (int q = warp; q < nrem; q += nwarps) {
+      double acc = 0.0;
+      if (tk != 0.0) {
+        const double* __restrict__ vk = hk;
+        const double* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
+        for (int64_t i = i_lo + lane; i < r_hi; i += 32) acc = fma(vk[i], aq[i], acc);
+        acc = warp_sum(acc);
+        if (own_k && lane == 0) acc += aq[k];
+      }
+      if (lane == 0) p_w[par][q] = acc;
+    }
+    cluster.sync();
+    if (tk != 0.0 && nrem > 0) {
+      for (int q = warp; q < nrem; q += nwarps) {
+        double w = 0.0;
+        for (int c = 0; c < ncta; ++c) w += cluster.map_shared_rank(&p_w[par][0], c)[q];
+        const double tw = tk * w;
+        const double* __restrict__ vk = hk;
+        double* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
+        if (own_k && lane == 0) aq[k] -= tw;
+        for (int64_t i = i_lo + lane; i < r_hi; i += 32) aq[i] = fma(-tw, vk[i], aq[i]);
+      }
+    }
+    __syncthreads();
+  }
+  // G[q][p] = v_qᵀ v_p (q < p) over this CTA's rows, then summed in CTA 0.
+  // Rows are staged through shared memory 64 at a time (coalesced loads);
+  // thread t accumulates pair t of the strictly upper triangle.
+  {
+    __shared__ double Vc[64][kQrNB + 1];
+    int pq = -1, pp = -1;
+    for (int p2 = 1, t = 0; p2 < nb && pq < 0; ++p2) {
+      if (tid < t + p2) { pq = tid - t; pp = p2; }
+      t += p2;
+    }
+    double acc = 0.0;
+    for (int64_t i0 = r_lo; i0 < r_hi; i0 += 64) {
+      for (int e = tid; e < 64 * kQrNB; e += blockDim.x) {
+        const int q = e / 64, ii = e % 64;
+        const int64_t i = i0 + ii;
+        Vc[ii][q] = (q < nb && i < r_hi) ? refl(h, mm, j0 + q, i) : 0.0;
+      }
+      __syncthreads();
+      if (pq >= 0) {
+#pragma unroll 8
+        for (int ii = 0; ii < 64; ++ii) acc = fma(Vc[ii][pq], Vc[ii][pp], acc);
+      }
+      __syncthreads();
+    }
+    if (pq >= 0) G[pq][pp] = acc;
+  }
+  cluster.sync();
+  if (rank == 0) {
+    __shared__ double Gs[kQrNB][kQrNB + 1];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int q = e / nb, pp = e % nb;
+      double g = 0.0;
+      if (q < pp)
+        for (int c = 0; c < ncta; ++c) g += cluster.map_shared_rank(&G[0][0], c)[q * (kQrNB + 1) + pp];
+      Gs[q][pp] = g;
+    }
+    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x) T[e / kQrNB][e % kQrNB] = 0.0;
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+      const int lane = threadIdx.x & 31;
+      for (int k = 0; k < nb; ++k) {
+        const double tk = tau[j0 + k];
+        double v = 0.0;
+        if (lane < k) {
+          for (int q = lane; q < k; ++q) v = fma(T[lane][q], Gs[q][k], v);
+          v = -tk * v;
+        }
+        __syncwarp();
+        if (lane < k) T[lane][k] = v;
+        if (lane == k) T[k][k] = tk;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
+      t_out[e] = T[e / kQrNB][e % kQrNB];
+  }
+  cluster.sync();  // CTA 0 has finished reading the others' shared memory
+}
+
+static bool qr_cluster_fits(int c) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, bool> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(dev, c);
+  auto it = known.find(key);
+  if (it != known.end()) return it->second;
+  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (ok) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)c);
+    cfg.blockDim = dim3(kQrCluThreads);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel, &cfg) == cudaSuccess &&
+         nclusters >= 1;
+  }
+  if (!ok) cudaGetLastError();
+  known[key] = ok;
+  return ok;
+}
+
+// 0 when the cluster kernel was launched, -1 when the caller must fall back.
+static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, double* h, double* tau,
+                                   double* t_out, cudaStream_t st) {
+  const int64_t rows = mm - j0;
+  int c = (int)((rows + 1023) / 1024);
+  c = c < 1 ? 1 : (c > kQrCluMax ? kQrCluMax : c);
+  if (!qr_cluster_fits(c)) return -1;
+  const int64_t r = (rows + c - 1) / c;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c);
+  cfg.blockDim = dim3(kQrCluThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)c;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel, mm, j0, pe, r, h, tau, t_out) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return 0;
 }
 
 // T (nb×nb, upper) of panel rows [j0, j0+nb): T[k][k] = tau_k and
@@ -423,9 +663,11 @@ extern "C" int lxgb_geqrf_f64(int64_t m, int64_t n, const double* a, int32_t a_l
   double* wbase = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + 256);
   for (int j0 = 0; j0 < nn; j0 += kQrNB) {
     const int nb = min(kQrNB, nn - j0);
-    qr_panel_kernel<<<1, kQrPanelThreads, 0, st>>>(m, nn, j0, j0 + nb, h, tau);
     double* Tp = t + (int64_t)(j0 / kQrNB) * kQrNB * kQrNB;
-    qr_larft_kernel<<<1, 512, 0, st>>>(m, j0, nb, h, tau, Tp);
+    if (launch_qr_panel_cluster(m, j0, j0 + nb, h, tau, Tp, st) != 0) {
+      qr_panel_kernel<<<1, kQrPanelThreads, 0, st>>>(m, nn, j0, j0 + nb, h, tau);
+      qr_larft_kernel<<<1, 512, 0, st>>>(m, j0, nb, h, tau, Tp);
+    }
     const int n2 = nn - (j0 + nb);
     if (n2 > 0) {
       int64_t split_len, used;
