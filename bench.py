@@ -624,8 +624,10 @@ def run_qr_ls(args):
 def run_cg_poisson(args):
     """CG on the 5-point -Laplacian of a 2048×2048 interior grid (zero
     Dirichlet boundary, matrix-free FunctionLinearOperator), 64 right-hand
-    sides: a timed block of iterations, plus the full solve to rtol 1e-10
-    with --cg-full."""
+    sides, rtol = atol = 1e-10: a timed block of iterations of the FP64 CG
+    (lineax's iteration statement for statement) and of the mixed-precision CG
+    (FP32 iterations, FP64 residual replacement every 8), plus the full
+    mixed-precision solve with --cg-full."""
     import torch
 
     from lineax_gb300 import _krylov
@@ -639,37 +641,46 @@ def run_cg_poisson(args):
     g = torch.Generator(device=dev).manual_seed(9)
     b = torch.randn(k, nx * ny, dtype=torch.float64, device=dev, generator=g)
     rtol, atol = 1e-10, 1e-10
-    _krylov.cg_block(op, b, rtol=rtol, atol=atol, max_steps=args.warmup)
-    torch.cuda.synchronize()
-    e0, e1 = _events(2)
-    e0.record()
-    res = _krylov.cg_block(op, b, rtol=rtol, atol=atol, max_steps=args.cg_iters)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    iters = max(res.steps)
     points = nx * ny * k
-    # bytes per point per iteration of this implementation (FP64 vectors):
-    # stencil reads p, writes Ap (16); alpha step reads Ap, p, x, r and writes
-    # x, r (48); beta step reads r, p and writes p (24); the true residual
-    # every 10th iteration adds b, Ax, r (2.4 amortised)
-    bpp = 16 + 48 + 24 + 2.4
-    gbs = bpp * points * iters / (ms * 1e-3) / 1e9
-    out = {"workload": f"cg_poisson_{nx}x{ny}_{k}rhs_f64", "metric": "CG iterations/s (64 RHS)",
-           "unit": "iterations/s", "value": iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
-           "iterations_timed": iters, "bytes_per_point_iteration": bpp,
-           "roofline": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
-                        "peak": 6784.0, "frac": gbs / 6784.0}}
-    if args.cg_full:
+    e0, e1 = _events(2)
+    out = {"workload": f"cg_poisson_{nx}x{ny}_{k}rhs", "metric": "CG iterations/s (64 RHS)",
+           "unit": "iterations/s", "rtol": rtol, "atol": atol}
+    # FP64 vectors: p, Ap read/written by the stencil (16), the alpha step reads
+    # Ap, p, x, r and writes x, r (48), the beta step reads r, p and writes p
+    # (24), the true residual every 10th iteration adds b, Ax, r (2.4)
+    for name, fn, bpp in (
+            ("fp64", lambda m: _krylov.cg_block(op, b, rtol=rtol, atol=atol, max_steps=m),
+             16 + 48 + 24 + 2.4),
+            # FP32 vectors: stencil reads p, writes Ap (8); update reads p, Ap,
+            # x_lo, r and writes x_lo, r (24); direction reads r, p, writes p
+            # (12); the FP64 replacement every 8 iterations (~48 / 8 = 6)
+            ("mixed", lambda m: _krylov.cg_poisson_mixed(op, b, rtol=rtol, atol=atol,
+                                                         max_steps=m), 8 + 24 + 12 + 6)):
+        fn(args.warmup)
+        torch.cuda.synchronize()
         e0.record()
-        res = _krylov.cg_block(op, b, rtol=rtol, atol=atol)
+        res = fn(args.cg_iters)
         e1.record()
         torch.cuda.synchronize()
-        y = res.y
-        r = b - op.mv_block(y)
-        out["full_solve"] = {"ms": e0.elapsed_time(e1), "iterations": max(res.steps),
-                             "results": sorted(set(res.results)),
-                             "max_rel_residual": float((r.abs().amax(1) / b.abs().amax(1)).max())}
+        ms = e0.elapsed_time(e1)
+        iters = max(res.steps)
+        gbs = bpp * points * iters / (ms * 1e-3) / 1e9
+        out[name] = {"iterations_per_s": iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+                     "iterations_timed": iters, "bytes_per_point_iteration": bpp,
+                     "roofline": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
+                                  "peak": 6784.0, "frac": gbs / 6784.0}}
+    out["value"] = out["mixed"]["iterations_per_s"]
+    if args.cg_full:
+        e0.record()
+        res = _krylov.cg_poisson_mixed(op, b, rtol=rtol, atol=atol)
+        e1.record()
+        torch.cuda.synchronize()
+        r = b - op.mv_block(res.y)
+        scale = atol + rtol * b.abs()
+        out["full_solve_mixed"] = {
+            "ms": e0.elapsed_time(e1), "iterations": max(res.steps),
+            "results": sorted(set(res.results)),
+            "max_residual_over_tolerance": float((r.abs() / scale).max())}
     print(json.dumps(out), flush=True)
 
 

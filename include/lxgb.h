@@ -361,6 +361,32 @@ int lxgb_gemv_df(int32_t m, int32_t n, const float* a_hi, const float* a_lo,
                  const double* b, double* y, int64_t ldy, int32_t mode,
                  void* work, int64_t work_bytes, void* stream);
 
+/* Mixed-precision CG for the 5-point Poisson operator (the matrix-free
+ * FunctionLinearOperator of lxgb_poisson5_f64 with scale 1) on an nx×ny grid,
+ * k right-hand sides: FP32 iteration vectors p, r, Ap and correction x_lo;
+ * FP64 solution x and right-hand side b (k vectors of nx*ny back to back).
+ * lxgb_cg32_refresh folds x_lo into x, replaces r by the FP64 true residual
+ * and applies lineax's max-norm stopping test to it (the solve of
+ * lineax/_solver/cg.py:114-227 with FP32 iterations between FP64 residual
+ * replacements; no reference counterpart as a precision mode).  Driver:
+ * init, refresh, start_direction, then (iterate, refresh) until status
+ * reports no active right-hand side.  status: 3 ints per right-hand side
+ * (active, steps, 0 running / max steps, 1 converged, 2 breakdown or NaN). */
+int64_t lxgb_cg32_workspace_size(int32_t nrhs);
+int lxgb_cg32_init(int32_t k, int64_t nx, int64_t ny, int64_t max_steps,
+                   void* work, int64_t work_bytes, void* stream);
+int lxgb_cg32_refresh(int32_t k, int64_t nx, int64_t ny, const double* b,
+                      double* x, float* xlo, float* r, double rtol, double atol,
+                      int64_t max_steps, void* work, int64_t work_bytes,
+                      void* stream);
+int lxgb_cg32_start_direction(int32_t k, int64_t n, const float* r, float* p,
+                              void* stream);
+int lxgb_cg32_iterate(int32_t k, int64_t nx, int64_t ny, int32_t iters,
+                      float* p, float* ap, float* xlo, float* r, void* work,
+                      int64_t work_bytes, void* stream);
+int lxgb_cg32_status(int32_t k, int32_t* out, void* work, int64_t work_bytes,
+                     void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */

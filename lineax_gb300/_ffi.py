@@ -89,6 +89,14 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i32, c_i32, c_i32, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, ctypes.c_float,
          ctypes.c_float, c_p, c_p]),
     "lxgb_getrs_f32": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_cg32_workspace_size": (c_i64, [c_i32]),
+    "lxgb_cg32_init": (ctypes.c_int, [c_i32, c_i64, c_i64, c_i64, c_p, c_i64, c_p]),
+    "lxgb_cg32_refresh": (ctypes.c_int, [c_i32, c_i64, c_i64, c_p, c_p, c_p, c_p, ctypes.c_double,
+                                         ctypes.c_double, c_i64, c_p, c_i64, c_p]),
+    "lxgb_cg32_start_direction": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p]),
+    "lxgb_cg32_iterate": (ctypes.c_int, [c_i32, c_i64, c_i64, c_i32, c_p, c_p, c_p, c_p, c_p,
+                                         c_i64, c_p]),
+    "lxgb_cg32_status": (ctypes.c_int, [c_i32, c_p, c_p, c_i64, c_p]),
     "lxgb_lu32_inverse_workspace_size": (c_i64, [c_i32, c_i32]),
     "lxgb_lu32_inverse": (ctypes.c_int, [c_i32, c_p, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64,
                                          c_p]),

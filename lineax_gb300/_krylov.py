@@ -132,6 +132,64 @@ def cg_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=N
     return KrylovResult(y, steps, results)
 
 
+def cg_poisson_mixed(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+                     check: int = 8, y0: torch.Tensor | None = None) -> KrylovResult:
+    """CG on a Poisson2DOperator (scale 1) for the (k, n) block b with FP32
+    iterations and an FP64 residual replacement every `check` iterations
+    (lxgb_cg32_*): the stopping test is lineax's max-norm test on the FP64
+    true residual, evaluated at the replacements.  HBM traffic per iteration
+    is that of FP32 vectors; the FP64 pipe sees only the replacements."""
+    if getattr(operator, "scale", None) != 1.0 or not hasattr(operator, "nx"):
+        raise ValueError("the mixed-precision CG needs a Poisson2DOperator with scale 1")
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    b = b.contiguous()
+    k, n = b.shape
+    nx, ny = operator.nx, operator.ny
+    if nx * ny != n:
+        raise ValueError("right-hand side length does not match the grid")
+    dev = b.device
+    max_steps_ = 10 * n if max_steps is None else int(max_steps)
+    x = torch.zeros_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone()
+    xlo = torch.zeros((k, n), dtype=torch.float32, device=dev)
+    r = torch.empty((k, n), dtype=torch.float32, device=dev)
+    p = torch.empty_like(r)
+    ap = torch.empty_like(r)
+    wbytes = int(_ffi.load().lxgb_cg32_workspace_size(k))
+    work = _work(wbytes, dev)
+    st = _stream(dev)
+    wb = work.numel() * 8
+    stat = torch.empty((k, 3), dtype=torch.int32, device=dev)
+    _ffi.call("lxgb_cg32_init", k, nx, ny, max_steps_, _ffi.ptr(work), wb, st)
+    _ffi.call("lxgb_cg32_refresh", k, nx, ny, _ffi.ptr(b), _ffi.ptr(x), _ffi.ptr(xlo), _ffi.ptr(r),
+              float(rtol), float(atol), max_steps_, _ffi.ptr(work), wb, st)
+    _ffi.call("lxgb_cg32_start_direction", k, n, _ffi.ptr(r), _ffi.ptr(p), st)
+    done = 0
+    while True:
+        _ffi.call("lxgb_cg32_status", k, _ffi.ptr(stat), _ffi.ptr(work), wb, st)
+        rows = stat.cpu().tolist()
+        if not any(row[0] for row in rows):
+            break
+        iters = max(1, min(int(check), max_steps_ - done))
+        _ffi.call("lxgb_cg32_iterate", k, nx, ny, iters, _ffi.ptr(p), _ffi.ptr(ap), _ffi.ptr(xlo),
+                  _ffi.ptr(r), _ffi.ptr(work), wb, st)
+        done += iters
+        _ffi.call("lxgb_cg32_refresh", k, nx, ny, _ffi.ptr(b), _ffi.ptr(x), _ffi.ptr(xlo),
+                  _ffi.ptr(r), float(rtol), float(atol), max_steps_, _ffi.ptr(work), wb, st)
+    results, steps = [], []
+    for _, s_, conv in rows:
+        if conv == 1:
+            res = SUCCESSFUL
+        elif conv == 2:
+            res = SINGULAR
+        else:
+            res = SINGULAR if max_steps is None else MAX_STEPS_REACHED
+        results.append(res)
+        steps.append(s_)
+    return KrylovResult(x, steps, results)
+
+
 def gmres_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
                 restart=20, stagnation_iters=20, preconditioner=None,
                 y0: torch.Tensor | None = None) -> KrylovResult:

@@ -24,10 +24,20 @@ class CG(AbstractLinearSolver):
     Options: ``preconditioner`` (a positive definite linear operator) and
     ``y0``, as in lineax.  ``norm`` must be ``max_norm`` (the device stopping
     test implements lineax's default norm).
+
+    ``precision="mixed"`` (an extension; Poisson2DOperator with scale 1, no
+    preconditioner): FP32 iterations with an FP64 true-residual replacement
+    every 8 iterations, stopping on lineax's test applied to that FP64
+    residual (`_krylov.cg_poisson_mixed`).  The default "fp64" follows
+    lineax's iteration statement for statement.
     """
 
     def __init__(self, rtol: float, atol: float, norm: Callable = max_norm,
-                 stabilise_every: int | None = 10, max_steps: int | None = None):
+                 stabilise_every: int | None = 10, max_steps: int | None = None,
+                 precision: str = "fp64"):
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
         if isinstance(rtol, (int, float)) and rtol < 0:
             raise ValueError("Tolerances must be non-negative.")
         if isinstance(atol, (int, float)) and atol < 0:
@@ -64,9 +74,16 @@ class CG(AbstractLinearSolver):
         b, _ = _krylov.vector_block(vector)
         y0b = None if "y0" not in options else _krylov.vector_block(y0)[0]
         pre = None if "preconditioner" not in options else preconditioner
-        res = _krylov.cg_block(operator, b, rtol=self.rtol, atol=self.atol,
-                               max_steps=self.max_steps, stabilise_every=self.stabilise_every,
-                               preconditioner=pre, y0=y0b)
+        if self.precision == "mixed":
+            if pre is not None:
+                raise ValueError("the mixed-precision CG takes no preconditioner")
+            res = _krylov.cg_poisson_mixed(operator, b, rtol=self.rtol, atol=self.atol,
+                                           max_steps=self.max_steps, y0=y0b)
+        else:
+            res = _krylov.cg_block(operator, b, rtol=self.rtol, atol=self.atol,
+                                   max_steps=self.max_steps,
+                                   stabilise_every=self.stabilise_every,
+                                   preconditioner=pre, y0=y0b)
         x = res.y[0]
         if is_nsd:
             x = -x

@@ -172,3 +172,31 @@ def test_cg_nonfinite_input_matches_reference(dev):
     assert sol.stats["num_steps"] == s_ref == 0
     sol = lx.linear_solve(lx.MatrixLinearOperator(t(a, dev)), t(b, dev), lx.LU(), throw=False)
     assert sol.result == lx.RESULTS.nonfinite_input
+
+
+@pytest.mark.parametrize("nx,ny,k", [(48, 40, 4), (130, 70, 3)])
+def test_cg_mixed_precision_poisson(dev, nx, ny, k):
+    """FP32 iterations with FP64 residual replacement: every right-hand side
+    ends on lineax's stopping test applied to the FP64 true residual, close to
+    the FP64 restatement's solution, and independent of the other right-hand
+    sides of the block."""
+    rng = np.random.default_rng(nx + ny)
+    b = rng.standard_normal((k, nx * ny))
+    a = poisson2d(nx, ny)
+    op = lx.Poisson2DOperator(nx, ny)
+    res = _krylov.cg_poisson_mixed(op, t(b, dev), rtol=1e-10, atol=1e-10)
+    y = res.y.cpu().numpy()
+    for c in range(k):
+        assert res.results[c] == 0
+        r = b[c] - a @ y[c]
+        assert np.all(np.abs(r) <= 1e-10 + 1e-10 * np.abs(b[c]))
+        x_ref, r_ref, s_ref = krylov.cg(lambda v: a @ v, b[c], rtol=1e-10, atol=1e-10)
+        np.testing.assert_allclose(y[c], x_ref, rtol=1e-6, atol=1e-8)
+        assert res.steps[c] <= 2 * s_ref + 16
+        alone = _krylov.cg_poisson_mixed(op, t(b[c:c + 1], dev), rtol=1e-10, atol=1e-10)
+        assert torch.equal(alone.y[0], res.y[c]) and alone.steps[0] == res.steps[c]
+    # through the solver API, and a max_steps cap
+    sol = lx.linear_solve(op, t(b[0], dev), lx.CG(rtol=1e-10, atol=1e-10, precision="mixed"))
+    assert sol.result == lx.RESULTS.successful
+    capped = _krylov.cg_poisson_mixed(op, t(b, dev), rtol=1e-10, atol=1e-10, max_steps=16)
+    assert all(s == 16 for s in capped.steps) and all(r_ == 1 for r_ in capped.results)
