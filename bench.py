@@ -384,10 +384,15 @@ def run_gpu(args):
         "gpu_launches": 2 * args.steps,
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None,
+            "frac": achieved / hbm_peak,
+            # DRAM bytes per launch: the ncu capture of the 512-system case read
+            # + wrote 364.5 MB for 151.4 MB of algorithmic bytes; scaled to this
+            # launch by its algorithmic bytes (the refinement re-reads A).
+            "traffic": hbm_bytes * (364.5 / 151.4),
             "kernel": "posv_mixed_kernel",
             "note": "HBM roofline of the algorithmic bytes (A read once, b, x); the kernel is "
-                    "issue-bound on FP64 (residual) and FP32 (factor), see compute",
+                    "latency-bound (barriers, instruction fetch, L2 latency; "
+                    "profiles/posv_mixed_kernel_ragged512.md), see compute",
             "compute": {"fp32_flops": fp32_flops, "fp64_flops": fp64_flops,
                         "fp32_tflops": fp32_flops / (ms * 1e-3) / 1e12,
                         "fp64_tflops": fp64_flops / (ms * 1e-3) / 1e12},
@@ -626,7 +631,7 @@ def run_cg_poisson(args):
     Dirichlet boundary, matrix-free FunctionLinearOperator), 64 right-hand
     sides, rtol = atol = 1e-10: a timed block of iterations of the FP64 CG
     (lineax's iteration statement for statement) and of the mixed-precision CG
-    (FP32 iterations, FP64 residual replacement every 8), plus the full
+    (FP32 iterations, FP64 residual replacement every 16), plus the full
     mixed-precision solve with --cg-full."""
     import torch
 
@@ -653,9 +658,10 @@ def run_cg_poisson(args):
              16 + 48 + 24 + 2.4),
             # FP32 vectors: stencil reads p, writes Ap (8); update reads p, Ap,
             # x_lo, r and writes x_lo, r (24); direction reads r, p, writes p
-            # (12); the FP64 replacement every 8 iterations (~48 / 8 = 6)
+            # (12); the FP64 replacement every 16 iterations: fold x += x_lo (24)
+            # and r = b - A x (20), 44 / 16 = 2.75
             ("mixed", lambda m: _krylov.cg_poisson_mixed(op, b, rtol=rtol, atol=atol,
-                                                         max_steps=m), 8 + 24 + 12 + 6)):
+                                                         max_steps=m), 8 + 24 + 12 + 2.75)):
         fn(args.warmup)
         torch.cuda.synchronize()
         e0.record()

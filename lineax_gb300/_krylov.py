@@ -133,7 +133,7 @@ def cg_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=N
 
 
 def cg_poisson_mixed(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
-                     check: int = 8, y0: torch.Tensor | None = None) -> KrylovResult:
+                     check: int = 16, y0: torch.Tensor | None = None) -> KrylovResult:
     """CG on a Poisson2DOperator (scale 1) for the (k, n) block b with FP32
     iterations and an FP64 residual replacement every `check` iterations
     (lxgb_cg32_*): the stopping test is lineax's max-norm test on the FP64

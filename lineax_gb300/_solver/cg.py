@@ -27,7 +27,7 @@ class CG(AbstractLinearSolver):
 
     ``precision="mixed"`` (an extension; Poisson2DOperator with scale 1, no
     preconditioner): FP32 iterations with an FP64 true-residual replacement
-    every 8 iterations, stopping on lineax's test applied to that FP64
+    every 16 iterations, stopping on lineax's test applied to that FP64
     residual (`_krylov.cg_poisson_mixed`).  The default "fp64" follows
     lineax's iteration statement for statement.
     """

@@ -1,7 +1,7 @@
 // Mixed-precision CG for the 5-point Poisson operator, k right-hand sides:
 // the iteration vectors p, r, Ap and the running correction x_lo are FP32
 // (the HBM stream of the hot loop), the solution x and the right-hand side b
-// FP64.  Every `check` iterations the host calls lxgb_cg32_refresh, which
+// FP64.  Every `check` iterations (16 by default) the host calls lxgb_cg32_refresh, which
 // folds x_lo into x in FP64, recomputes the true residual r = b - A x in FP64
 // (residual replacement: the recurrence residual restarts from it, the search
 // direction is kept), evaluates lineax's stopping test on that true residual
@@ -189,59 +189,7 @@ __device__ __forceinline__ int c32_ratio_code(double v, double sc) {
   return av > sb ? 1 : 0;
 }
 
-// Refresh (active right-hand sides): x += x_lo, x_lo = 0, r = b - A x in
-// FP64 (stored as FP32), partial <r, r> and the stopping-test code.
-__global__ void __launch_bounds__(kC32Threads)
-c32_refresh_kernel(int64_t nx, int64_t ny, C32State s, const double* __restrict__ b,
-                   double* __restrict__ x, float* __restrict__ xlo, float* __restrict__ r,
-                   int* __restrict__ codes, double rtol, double atol) {
-  __shared__ double sm[kC32Threads / 32];
-  __shared__ int s_code;
-  const int c = blockIdx.z;
-  const int part = blockIdx.y * gridDim.x + blockIdx.x;
-  if (!s.act[c]) return;
-  const int64_t n = nx * ny;
-  const int64_t o0 = (int64_t)c * n;
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (threadIdx.x == 0) s_code = 0;
-  __syncthreads();
-  // the residual of x + x_lo (x itself is updated by c32_fold_kernel after
-  // every CTA has read its neighbours)
-  const int64_t i0 = (int64_t)blockIdx.y * kC32RowsPerCta;
-  const int64_t i1 = min(nx, i0 + kC32RowsPerCta);
-  float acc = 0.0f;
-  int code = 0;
-  if (j < ny) {
-    auto xv = [&](int64_t i, int64_t jj) -> double {
-      const int64_t o = o0 + i * ny + jj;
-      return x[o] + (double)xlo[o];
-    };
-    for (int64_t i = i0; i < i1; ++i) {
-      const int64_t o = o0 + i * ny + j;
-      const double cen = xv(i, j);
-      const double up = (i > 0) ? xv(i - 1, j) : 0.0;
-      const double dn = (i + 1 < nx) ? xv(i + 1, j) : 0.0;
-      const double lf = (j > 0) ? xv(i, j - 1) : 0.0;
-      const double rt = (j + 1 < ny) ? xv(i, j + 1) : 0.0;
-      const double ax = fma(4.0, cen, -((up + dn) + (lf + rt)));
-      const double rv = b[o] - ax;
-      const float rf = (float)rv;
-      r[o] = rf;
-      acc = fmaf(rf, rf, acc);
-      code = max(code, c32_ratio_code(rv, fma(rtol, fabs(b[o]), atol)));
-    }
-  }
-  const double t = c32_block_sum((double)acc, sm);
-  if (code) atomicMax(&s_code, code);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s.part[(int64_t)c * kC32MaxParts + part] = t;
-    codes[(int64_t)c * kC32MaxParts + part] = s_code;
-  }
-}
-
-// Second half of the refresh: x += x_lo and x_lo = 0 (after every CTA has
-// read the neighbours it needed).
+// Refresh, first pass (active right-hand sides): x += x_lo, x_lo = 0.
 __global__ void c32_fold_kernel(int64_t n, C32State s, double* __restrict__ x,
                                 float* __restrict__ xlo) {
   const int c = blockIdx.y;
@@ -251,6 +199,54 @@ __global__ void c32_fold_kernel(int64_t n, C32State s, double* __restrict__ x,
        i += (int64_t)gridDim.x * blockDim.x) {
     x[o + i] += (double)xlo[o + i];
     xlo[o + i] = 0.0f;
+  }
+}
+
+// Refresh, second pass: r = b - A x in FP64 (stored as FP32), partial <r, r>
+// and the stopping-test code per CTA.
+__global__ void __launch_bounds__(kC32Threads)
+c32_refresh_kernel(int64_t nx, int64_t ny, C32State s, const double* __restrict__ b,
+                   const double* __restrict__ x, float* __restrict__ r,
+                   int* __restrict__ codes, double rtol, double atol) {
+  __shared__ double sm[kC32Threads / 32];
+  __shared__ int s_code;
+  const int c = blockIdx.z;
+  const int part = blockIdx.y * gridDim.x + blockIdx.x;
+  if (!s.act[c]) return;
+  const int64_t n = nx * ny;
+  const double* xc = x + (int64_t)c * n;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x == 0) s_code = 0;
+  __syncthreads();
+  const int64_t i0 = (int64_t)blockIdx.y * kC32RowsPerCta;
+  const int64_t i1 = min(nx, i0 + kC32RowsPerCta);
+  float acc = 0.0f;
+  int code = 0;
+  if (j < ny) {
+    double up = (i0 > 0) ? xc[(i0 - 1) * ny + j] : 0.0;
+    double cen = xc[i0 * ny + j];
+    for (int64_t i = i0; i < i1; ++i) {
+      const int64_t o = i * ny + j;
+      const double dn = (i + 1 < nx) ? xc[o + ny] : 0.0;
+      const double lf = (j > 0) ? xc[o - 1] : 0.0;
+      const double rt = (j + 1 < ny) ? xc[o + 1] : 0.0;
+      const double ax = fma(4.0, cen, -((up + dn) + (lf + rt)));
+      const double bv = b[(int64_t)c * n + o];
+      const double rv = bv - ax;
+      const float rf = (float)rv;
+      r[(int64_t)c * n + o] = rf;
+      acc = fmaf(rf, rf, acc);
+      code = max(code, c32_ratio_code(rv, fma(rtol, fabs(bv), atol)));
+      up = cen;
+      cen = dn;
+    }
+  }
+  const double t = c32_block_sum((double)acc, sm);
+  if (code) atomicMax(&s_code, code);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s.part[(int64_t)c * kC32MaxParts + part] = t;
+    codes[(int64_t)c * kC32MaxParts + part] = s_code;
   }
 }
 
@@ -350,9 +346,9 @@ extern "C" int lxgb_cg32_refresh(int32_t k, int64_t nx, int64_t ny, const double
   dim3 g((unsigned)((ny + kC32Threads - 1) / kC32Threads),
          (unsigned)((nx + kC32RowsPerCta - 1) / kC32RowsPerCta), (unsigned)k);
   const int P = c32_parts(nx, ny);
-  c32_refresh_kernel<<<g, kC32Threads, 0, st>>>(nx, ny, s, b, x, xlo, r, codes, rtol, atol);
   c32_fold_kernel<<<dim3((unsigned)c32_vec_grid(nx * ny), (unsigned)k), kC32Threads, 0, st>>>(
       nx * ny, s, x, xlo);
+  c32_refresh_kernel<<<g, kC32Threads, 0, st>>>(nx, ny, s, b, x, r, codes, rtol, atol);
   c32_refresh_final_kernel<<<k, 32, 0, st>>>(k, s, codes, P, max_steps);
   return check_launch("cg32_refresh");
 }
