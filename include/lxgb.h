@@ -387,6 +387,18 @@ int lxgb_cg32_iterate(int32_t k, int64_t nx, int64_t ny, int32_t iters,
 int lxgb_cg32_status(int32_t k, int32_t* out, void* work, int64_t work_bytes,
                      void* stream);
 
+/* Householder QR of a tall FP64 matrix A (m × n row-major, n <= m, m % 4 ==
+ * 0) in FP32 with the trailing updates on the tcgen05 tensor cores (TF32
+ * products): h (n × m FP32) in the raw layout of lxgb_geqrf_f64, tau (n),
+ * t (lxgb_geqrf_t_elems(n) FP32: each panel's compact-WY T).  h 16-byte and
+ * work 256-byte aligned; *err is set if a tensor-core pipeline wait gave up.
+ * The factor of the mixed-precision least-squares solve (no reference
+ * counterpart as a precision mode of lineax/_solver/qr.py:55-118). */
+int64_t lxgb_geqrf_f32_tc_workspace_size(int64_t m, int64_t n);
+int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                      float* t, int32_t* err, void* work, int64_t work_bytes,
+                      void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */
 /* ------------------------------------------------------------------------ */

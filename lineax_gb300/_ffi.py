@@ -89,6 +89,8 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i32, c_i32, c_i32, c_p, c_p, c_i64, c_p, c_p, c_i64, c_p, c_i64, ctypes.c_float,
          ctypes.c_float, c_p, c_p]),
     "lxgb_getrs_f32": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_geqrf_f32_tc_workspace_size": (c_i64, [c_i64, c_i64]),
+    "lxgb_geqrf_f32_tc": (ctypes.c_int, [c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_i64, c_p]),
     "lxgb_cg32_workspace_size": (c_i64, [c_i32]),
     "lxgb_cg32_init": (ctypes.c_int, [c_i32, c_i64, c_i64, c_i64, c_p, c_i64, c_p]),
     "lxgb_cg32_refresh": (ctypes.c_int, [c_i32, c_i64, c_i64, c_p, c_p, c_p, c_p, ctypes.c_double,

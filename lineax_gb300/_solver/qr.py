@@ -19,7 +19,17 @@ from .misc import pack_structures, ravel_vector, transpose_packed_structures, un
 
 class QR(AbstractLinearSolver):
     """QR solver: least squares for tall operators, minimum norm for wide ones,
-    the usual solution for square nonsingular ones (full rank assumed)."""
+    the usual solution for square nonsingular ones (full rank assumed).
+
+    ``precision="mixed"`` (an extension, tall operators with a row count that
+    is a multiple of 4): TF32 tensor-core QR and corrected semi-normal
+    equations refined to FP64 accuracy (``mixed.qr_lstsq``); other shapes use
+    the FP64 path."""
+
+    def __init__(self, precision: str = "fp64"):
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
 
     def __repr__(self):
         return "QR()"
@@ -28,12 +38,25 @@ class QR(AbstractLinearSolver):
         matrix = operator.as_matrix()
         m, n = matrix.shape
         transpose = n > m
+        if self.precision == "mixed" and not transpose and m % 4 == 0:
+            from .. import mixed
+
+            a64 = matrix.to(torch.float64).contiguous()
+            return (mixed.qr_factor_tf32(a64), a64), "mixed", pack_structures(operator)
         # QR.init factors M = matrix (tall) or M = matrixᵀ (wide, qr.py:59-61);
         # h = Mᵀ is `matrix` itself in the wide case.
         h, tau, t = _dense.geqrf(matrix, already_transposed=transpose)
         return (h, tau, t), transpose, pack_structures(operator)
 
     def compute(self, state, vector, options):
+        if state[1] == "mixed":
+            from .. import mixed
+
+            (factor, a64), _, packed = state
+            b = ravel_vector(vector, packed)
+            res = mixed.qr_lstsq(a64, b, factor=factor)
+            return unravel_solution(res.x[0], packed), RESULTS.successful, {
+                "refinement_steps": res.iters}
         (h, tau, t), transpose, packed = state
         b = ravel_vector(vector, packed)
         n_min, n_full = h.shape
@@ -50,6 +73,8 @@ class QR(AbstractLinearSolver):
         return unravel_solution(x, packed), RESULTS.successful, {}
 
     def transpose(self, state, options):
+        if state[1] == "mixed":
+            raise NotImplementedError("transpose of the mixed-precision QR state")
         factor, transpose, packed = state
         return (factor, not transpose, transpose_packed_structures(packed)), {}
 

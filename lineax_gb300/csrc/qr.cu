@@ -26,6 +26,7 @@
 #include <utility>
 
 #include "common.cuh"
+#include "tc_gemm.cuh"
 
 namespace lxgb {
 
@@ -33,8 +34,9 @@ constexpr int kQrNB = 32;
 constexpr int kQrPanelThreads = 512;
 
 // v_p[i] for panel row p (global row r = j0 + p) read from h.
-__device__ __forceinline__ double refl(const double* h, int64_t mm, int r, int64_t i) {
-  return (i < r) ? 0.0 : (i == r ? 1.0 : h[(int64_t)r * mm + i]);
+template <typename T>
+__device__ __forceinline__ T refl(const T* h, int64_t mm, int r, int64_t i) {
+  return (i < r) ? T(0) : (i == r ? T(1) : h[(int64_t)r * mm + i]);
 }
 
 __device__ double block_sum(double v, double* red) {
@@ -123,17 +125,17 @@ constexpr int kQrCluMax = 16;
 
 // Block-wide sums of NV values per thread, written to out[0..NV) (thread 0's
 // view is complete after the trailing barrier).  red: [warps][NV].
-template <int NV>
-__device__ void block_sums(double (&v)[NV], double (*red)[kQrNB], double* out) {
+template <int NV, typename T>
+__device__ void block_sums(T (&v)[NV], T (*red)[kQrNB], T* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
-    const double s = warp_sum(v[q]);
+    const T s = warp_sum(v[q]);
     if (lane == 0) red[warp][q] = s;
   }
   __syncthreads();
   for (int q = threadIdx.x; q < NV; q += blockDim.x) {
-    double t = 0.0;
+    T t = T(0);
     for (int w = 0; w < nw; ++w) t += red[w][q];
     out[q] = t;
   }
@@ -150,16 +152,16 @@ __device__ void block_sums(double (&v)[NV], double (*red)[kQrNB], double* out) {
 // Partials are double-buffered by column parity: two barriers per column.
 // Then G = VᵀV from per-CTA partials and T by larft's recurrence in CTA 0.
 // Same rules as qr_panel_kernel + qr_larft_kernel (LAPACK geqr2/larfg/larft).
+template <typename T>
 __global__ void __launch_bounds__(kQrCluThreads, 1)
 qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
-                        double* __restrict__ h, double* __restrict__ tau,
-                        double* __restrict__ t_out) {
-  __shared__ double red[kQrCluThreads / 32][kQrNB];
-  __shared__ double p_ss[2], p_alpha[2];
-  __shared__ double p_w[2][kQrNB];
-  __shared__ double G[kQrNB][kQrNB + 1];
-  __shared__ double T[kQrNB][kQrNB + 1];
-  __shared__ double s_tau, s_scal;
+                        T* __restrict__ h, T* __restrict__ tau, T* __restrict__ t_out) {
+  __shared__ T red[kQrCluThreads / 32][kQrNB];
+  __shared__ T p_ss[2], p_alpha[2];
+  __shared__ T p_w[2][kQrNB];
+  __shared__ T G[kQrNB][kQrNB + 1];
+  __shared__ T Tm[kQrNB][kQrNB + 1];
+  __shared__ T s_tau, s_scal;
   cg::cluster_group cluster = cg::this_cluster();
   const int ncta = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
@@ -169,48 +171,48 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
   const int64_t r_hi = min(mm, r_lo + rows_per_cta);
   for (int k = j0; k < pe; ++k) {
     const int par = (k - j0) & 1;
-    double* hk = h + (int64_t)k * mm;
+    T* hk = h + (int64_t)k * mm;
     const bool own_k = (k >= r_lo && k < r_hi);
-    double ss[1] = {0.0};
+    T ss[1] = {T(0)};
     for (int64_t i = max((int64_t)k + 1, r_lo) + tid; i < r_hi; i += blockDim.x)
       ss[0] = fma(hk[i], hk[i], ss[0]);
     block_sums<1>(ss, red, &p_ss[par]);
     if (tid == 0 && own_k) p_alpha[par] = hk[k];
     cluster.sync();
     if (tid == 0) {
-      double xnorm2 = 0.0;
+      T xnorm2 = T(0);
       for (int c = 0; c < ncta; ++c) xnorm2 += *cluster.map_shared_rank(&p_ss[par], c);
       const int own = (int)((k - j0) / rows_per_cta);
-      const double alpha = *cluster.map_shared_rank(&p_alpha[par], own);
-      const double xnorm = sqrt(xnorm2);
-      if (xnorm == 0.0) {
-        s_tau = 0.0;
-        s_scal = 1.0;
+      const T alpha = *cluster.map_shared_rank(&p_alpha[par], own);
+      const T xnorm = sqrt(xnorm2);
+      if (xnorm == T(0)) {
+        s_tau = T(0);
+        s_scal = T(1);
       } else {
-        const double beta = -copysign(hypot(alpha, xnorm), alpha);
+        const T beta = -copysign(hypot(alpha, xnorm), alpha);
         s_tau = (beta - alpha) / beta;
-        s_scal = 1.0 / (alpha - beta);
+        s_scal = T(1) / (alpha - beta);
         if (own_k) hk[k] = beta;
       }
       if (rank == 0) tau[k] = s_tau;
     }
     __syncthreads();
-    const double tk = s_tau;
+    const T tk = s_tau;
     const int nrem = pe - k - 1;
     const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int64_t i_lo = max((int64_t)k + 1, r_lo);
-    if (tk != 0.0) {
-      const double sc = s_scal;
+    if (tk != T(0)) {
+      const T sc = s_scal;
       for (int64_t i = i_lo + tid; i < r_hi; i += blockDim.x) hk[i] *= sc;
     }
     __syncthreads();
     // one warp per trailing column: w_q partial = v_kᵀ a_q over this CTA's
     // rows (+ a_q[k] from the owner of row k, as v_k[k] = 1)
     for (int q = warp; q < nrem; q += nwarps) {
-      double acc = 0.0;
-      if (tk != 0.0) {
-        const double* __restrict__ vk = hk;
-        const double* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
+      T acc = T(0);
+      if (tk != T(0)) {
+        const T* __restrict__ vk = hk;
+        const T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
         for (int64_t i = i_lo + lane; i < r_hi; i += 32) acc = fma(vk[i], aq[i], acc);
         acc = warp_sum(acc);
         if (own_k && lane == 0) acc += aq[k];
@@ -218,13 +220,13 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
       if (lane == 0) p_w[par][q] = acc;
     }
     cluster.sync();
-    if (tk != 0.0 && nrem > 0) {
+    if (tk != T(0) && nrem > 0) {
       for (int q = warp; q < nrem; q += nwarps) {
-        double w = 0.0;
+        T w = T(0);
         for (int c = 0; c < ncta; ++c) w += cluster.map_shared_rank(&p_w[par][0], c)[q];
-        const double tw = tk * w;
-        const double* __restrict__ vk = hk;
-        double* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
+        const T tw = tk * w;
+        const T* __restrict__ vk = hk;
+        T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
         if (own_k && lane == 0) aq[k] -= tw;
         for (int64_t i = i_lo + lane; i < r_hi; i += 32) aq[i] = fma(-tw, vk[i], aq[i]);
       }
@@ -235,18 +237,18 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
   // Rows are staged through shared memory 64 at a time (coalesced loads);
   // thread t accumulates pair t of the strictly upper triangle.
   {
-    __shared__ double Vc[64][kQrNB + 1];
+    __shared__ T Vc[64][kQrNB + 1];
     int pq = -1, pp = -1;
     for (int p2 = 1, t = 0; p2 < nb && pq < 0; ++p2) {
       if (tid < t + p2) { pq = tid - t; pp = p2; }
       t += p2;
     }
-    double acc = 0.0;
+    T acc = T(0);
     for (int64_t i0 = r_lo; i0 < r_hi; i0 += 64) {
       for (int e = tid; e < 64 * kQrNB; e += blockDim.x) {
         const int q = e / 64, ii = e % 64;
         const int64_t i = i0 + ii;
-        Vc[ii][q] = (q < nb && i < r_hi) ? refl(h, mm, j0 + q, i) : 0.0;
+        Vc[ii][q] = (q < nb && i < r_hi) ? refl(h, mm, j0 + q, i) : T(0);
       }
       __syncthreads();
       if (pq >= 0) {
@@ -259,38 +261,39 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
   }
   cluster.sync();
   if (rank == 0) {
-    __shared__ double Gs[kQrNB][kQrNB + 1];
+    __shared__ T Gs[kQrNB][kQrNB + 1];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
       const int q = e / nb, pp = e % nb;
-      double g = 0.0;
+      T g = T(0);
       if (q < pp)
         for (int c = 0; c < ncta; ++c) g += cluster.map_shared_rank(&G[0][0], c)[q * (kQrNB + 1) + pp];
       Gs[q][pp] = g;
     }
-    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x) T[e / kQrNB][e % kQrNB] = 0.0;
+    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x) Tm[e / kQrNB][e % kQrNB] = T(0);
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
       const int lane = threadIdx.x & 31;
       for (int k = 0; k < nb; ++k) {
-        const double tk = tau[j0 + k];
-        double v = 0.0;
+        const T tk = tau[j0 + k];
+        T v = T(0);
         if (lane < k) {
-          for (int q = lane; q < k; ++q) v = fma(T[lane][q], Gs[q][k], v);
+          for (int q = lane; q < k; ++q) v = fma(Tm[lane][q], Gs[q][k], v);
           v = -tk * v;
         }
         __syncwarp();
-        if (lane < k) T[lane][k] = v;
-        if (lane == k) T[k][k] = tk;
+        if (lane < k) Tm[lane][k] = v;
+        if (lane == k) Tm[k][k] = tk;
         __syncwarp();
       }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
-      t_out[e] = T[e / kQrNB][e % kQrNB];
+      t_out[e] = Tm[e / kQrNB][e % kQrNB];
   }
   cluster.sync();  // CTA 0 has finished reading the others' shared memory
 }
 
+template <typename T>
 static bool qr_cluster_fits(int c) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, bool> known;
@@ -300,7 +303,7 @@ static bool qr_cluster_fits(int c) {
   const auto key = std::make_pair(dev, c);
   auto it = known.find(key);
   if (it != known.end()) return it->second;
-  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel,
+  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel<T>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
   if (ok) {
     cudaLaunchConfig_t cfg = {};
@@ -314,7 +317,8 @@ static bool qr_cluster_fits(int c) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel, &cfg) == cudaSuccess &&
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel<T>, &cfg) ==
+             cudaSuccess &&
          nclusters >= 1;
   }
   if (!ok) cudaGetLastError();
@@ -323,12 +327,13 @@ static bool qr_cluster_fits(int c) {
 }
 
 // 0 when the cluster kernel was launched, -1 when the caller must fall back.
-static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, double* h, double* tau,
-                                   double* t_out, cudaStream_t st) {
+template <typename T>
+static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* t_out,
+                                   cudaStream_t st) {
   const int64_t rows = mm - j0;
   int c = (int)((rows + 1023) / 1024);
   c = c < 1 ? 1 : (c > kQrCluMax ? kQrCluMax : c);
-  if (!qr_cluster_fits(c)) return -1;
+  if (!qr_cluster_fits<T>(c)) return -1;
   const int64_t r = (rows + c - 1) / c;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c);
@@ -341,7 +346,7 @@ static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, double* h, double
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel, mm, j0, pe, r, h, tau, t_out) !=
+  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel<T>, mm, j0, pe, r, h, tau, t_out) !=
       cudaSuccess) {
     cudaGetLastError();
     return -1;
@@ -717,4 +722,148 @@ extern "C" int lxgb_ormqr_f64(int64_t m, int64_t n, const double* h, const doubl
     ormqr_apply_kernel<<<g, 256, 0, st>>>(m, j0, nb, h, Tp, trans, c, nchunks, part);
   }
   return check_launch("ormqr");
+}
+
+namespace lxgb {
+
+// ---------------------------------------------------------------------------
+// FP32 Householder QR with the trailing updates on the tcgen05 tensor cores
+// (TF32 products): the factor of the mixed-precision least-squares solver.
+// Same raw layout as lxgb_geqrf_f64 (h = Mᵀ, n rows of length m, FP32), same
+// 32-column panels (the cluster panel kernel in FP32, with its T), then per
+// panel, with V the panel's reflectors (zeros above the diagonal, ones on it)
+// and C the trailing rows of h:
+//   W  = C Vᵀ        (n2 × 32; tcgen05, the K = m range split in chunks)
+//   W' = W T         (fold the chunks and multiply by T on the CUDA cores)
+//   C -= W' V        (tcgen05, a rank-32 update of the trailing rows)
+// ---------------------------------------------------------------------------
+constexpr int kQr32Split = 8;
+
+// vrows[p][i] = v_p[i] (32 × m, row stride m) and vcols[i][p] (m × 32).
+__global__ void qr32_make_v_kernel(int64_t mm, int j0, int nb, const float* __restrict__ h,
+                                   float* __restrict__ vrows, float* __restrict__ vcols) {
+  const int64_t total = (int64_t)kQrNB * mm;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(e / mm);
+    const int64_t i = e % mm;
+    const float v = (p < nb) ? refl(h, mm, j0 + p, i) : 0.0f;
+    vrows[(int64_t)p * mm + i] = v;
+    vcols[i * kQrNB + p] = v;
+  }
+}
+
+// w2[j][p] = sum_q (sum_s wpart[s][j][q]) T[q][p], j < n2.
+__global__ void qr32_wt_kernel(int n2, int nb, int splits, const float* __restrict__ wpart,
+                               const float* __restrict__ T, float* __restrict__ w2) {
+  __shared__ float Ts[kQrNB][kQrNB + 1];
+  for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
+    Ts[e / kQrNB][e % kQrNB] = T[e];
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n2) return;
+  float w[kQrNB];
+#pragma unroll
+  for (int q = 0; q < kQrNB; ++q) w[q] = 0.0f;
+  for (int sp = 0; sp < splits; ++sp) {
+#pragma unroll
+    for (int q = 0; q < kQrNB; ++q)
+      if (q < nb) w[q] += wpart[((int64_t)sp * n2 + j) * kQrNB + q];
+  }
+#pragma unroll
+  for (int p = 0; p < kQrNB; ++p) {
+    float a = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kQrNB; ++q) a = fmaf(w[q], Ts[q][p], a);
+    w2[(int64_t)j * kQrNB + p] = (p < nb) ? a : 0.0f;
+  }
+}
+
+__global__ void qr32_transpose_cvt_kernel(int64_t rows, int64_t cols, const double* __restrict__ a,
+                                          float* __restrict__ h) {
+  __shared__ float tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t r = r0 + k, c = c0 + threadIdx.x;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? (float)a[r * cols + c] : 0.0f;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int64_t c = c0 + k, r = r0 + threadIdx.x;
+    if (c < cols && r < rows) h[c * rows + r] = tile[threadIdx.x][k];
+  }
+}
+
+static int64_t qr32_align(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+}  // namespace lxgb
+
+extern "C" int64_t lxgb_geqrf_f32_tc_workspace_size(int64_t m, int64_t n) {
+  using namespace lxgb;
+  const int64_t v = qr32_align((int64_t)kQrNB * m * 4);
+  const int64_t wp = qr32_align((int64_t)kQr32Split * (n > 0 ? n : 1) * kQrNB * 4);
+  const int64_t w2 = qr32_align((int64_t)(n > 0 ? n : 1) * kQrNB * 4);
+  return 256 + 2 * v + wp + w2;
+}
+
+extern "C" int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                                 float* t, int32_t* err, void* work, int64_t work_bytes,
+                                 void* stream) {
+  using namespace lxgb;
+  LXGB_REQUIRE(m >= 0 && n >= 0, "geqrf_f32_tc: negative size");
+  LXGB_REQUIRE(n <= m, "geqrf_f32_tc: needs a tall matrix (n <= m)");
+  if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(a && h && tau && t && err && work, "geqrf_f32_tc: null pointer");
+  LXGB_REQUIRE((m % 4) == 0, "geqrf_f32_tc: m must be a multiple of 4 (16-byte TMA rows)");
+  LXGB_REQUIRE(m < (1LL << 31) && n < (1LL << 31), "geqrf_f32_tc: too large");
+  LXGB_REQUIRE((((uintptr_t)h) & 15) == 0 && (((uintptr_t)work) & 255) == 0,
+               "geqrf_f32_tc: h must be 16-byte and work 256-byte aligned");
+  if (work_bytes < lxgb_geqrf_f32_tc_workspace_size(m, n)) {
+    set_last_error("geqrf_f32_tc: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  {
+    dim3 grid((unsigned)((n + 31) / 32), (unsigned)((m + 31) / 32));
+    qr32_transpose_cvt_kernel<<<grid, dim3(32, 8), 0, st>>>(m, n, a, h);
+  }
+  const int64_t vb = qr32_align((int64_t)kQrNB * m * 4);
+  const int64_t wpb = qr32_align((int64_t)kQr32Split * n * kQrNB * 4);
+  char* wb = reinterpret_cast<char*>(work) + 256;
+  float* vrows = reinterpret_cast<float*>(wb);
+  float* vcols = reinterpret_cast<float*>(wb + vb);
+  float* wpart = reinterpret_cast<float*>(wb + 2 * vb);
+  float* w2 = reinterpret_cast<float*>(wb + 2 * vb + wpb);
+  const int nn = (int)n;
+  for (int j0 = 0; j0 < nn; j0 += kQrNB) {
+    const int nb = min(kQrNB, nn - j0);
+    float* Tp = t + (int64_t)(j0 / kQrNB) * kQrNB * kQrNB;
+    if (launch_qr_panel_cluster<float>(m, j0, j0 + nb, h, tau, Tp, st) != 0) {
+      set_last_error("geqrf_f32_tc: the panel's thread-block cluster cannot be scheduled");
+      return LXGB_NOT_SUPPORTED;
+    }
+    const int n2 = nn - (j0 + nb);
+    if (n2 <= 0) continue;
+    const int64_t tot = (int64_t)kQrNB * m;
+    qr32_make_v_kernel<<<(unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096), 256, 0,
+                         st>>>(m, j0, nb, h, vrows, vcols);
+    float* c = h + (int64_t)(j0 + nb) * m;  // trailing rows of h
+    const int64_t klen = m - j0;
+    const int64_t chunk = ((klen + kQr32Split - 1) / kQr32Split + 31) / 32 * 32;
+    int used = 0;
+    for (int sp = 0; sp < kQr32Split; ++sp) {
+      const int64_t k0 = j0 + (int64_t)sp * chunk;
+      if (k0 >= m) break;
+      const int64_t kl = min(chunk, m - k0);
+      int rc = gemm_tf32_nt(n2, nb, (int)kl, c + k0, m, vrows + k0, m,
+                            wpart + (int64_t)sp * n2 * kQrNB, kQrNB, 1.0f, 0.0f, err, st);
+      if (rc) return rc;
+      ++used;
+    }
+    qr32_wt_kernel<<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(n2, nb, used, wpart, Tp, w2);
+    int rc = gemm_tf32_nt(n2, (int)klen, nb, w2, kQrNB, vcols + (int64_t)j0 * kQrNB, kQrNB,
+                          c + j0, m, -1.0f, 1.0f, err, st);
+    if (rc) return rc;
+  }
+  return check_launch("geqrf_f32_tc");
 }

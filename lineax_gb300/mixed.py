@@ -370,3 +370,106 @@ def _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps) -> IR
     x = _dense.lu_solve(lu, piv, b64)
     berr = _berr(outer_op.residual(x, b64), x, anorm, bnorm)
     return IRResult(x, berr, it, inner_steps, all(e <= tol for e in berr), fallback=True)
+
+
+# ---------------------------------------------------------------------------
+# Mixed-precision least squares: TF32 tensor-core QR + corrected semi-normal
+# equations refined in FP64-accurate arithmetic.
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class QR32:
+    h: torch.Tensor     # n × m FP32, jnp.linalg.qr(mode="raw") layout (h = Aᵀ factored)
+    tau: torch.Tensor   # n FP32
+    t: torch.Tensor     # compact-WY T of each 32-column panel
+    rt: torch.Tensor    # Rᵀ (n × n, lower, FP64) for the FP64 triangular solves
+
+
+def qr_factor_tf32(a: torch.Tensor) -> QR32:
+    """Householder QR of a tall A (m × n, m % 4 == 0) in FP32 with the
+    trailing updates on the tcgen05 tensor cores (lxgb_geqrf_f32_tc)."""
+    a64 = as_device_f64(a).contiguous()
+    m, n = a64.shape
+    if n > m or m % 4:
+        raise ValueError("qr_factor_tf32 needs a tall matrix with m a multiple of 4")
+    dev = a64.device
+    lib = _ffi.load()
+    h = torch.empty((n, m), dtype=torch.float32, device=dev)
+    tau = torch.empty(n, dtype=torch.float32, device=dev)
+    t = torch.empty(max(1, int(lib.lxgb_geqrf_t_elems(n))), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    wbytes = int(lib.lxgb_geqrf_f32_tc_workspace_size(m, n))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    _ffi.call("lxgb_geqrf_f32_tc", m, n, _ffi.ptr(a64), _ffi.ptr(h), _ffi.ptr(tau), _ffi.ptr(t),
+              _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8, _ffi.stream_handle(dev))
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the QR update")
+    rt = h[:, :n].double().contiguous()
+    return QR32(h, tau, t, rt)
+
+
+def _gemv_df(split: SplitMatrix, x: torch.Tensor, b: torch.Tensor | None) -> torch.Tensor:
+    """y = A x or b - A x for a rectangular SplitMatrix A (rows × cols) and a
+    (k, cols) block x, in double-float arithmetic."""
+    rows, cols = split.hi.shape
+    xb = x.contiguous()
+    k = xb.shape[0]
+    out = torch.empty((k, rows), dtype=torch.float64, device=xb.device)
+    wbytes = int(_ffi.load().lxgb_gemv_df_workspace_size(cols, k))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=xb.device)
+    _ffi.call("lxgb_gemv_df", rows, cols, _ffi.ptr(split.hi), _ffi.ptr(split.lo), cols, k,
+              _ffi.ptr(xb), cols, _ffi.ptr(b), _ffi.ptr(out), rows, 1, _ffi.ptr(work),
+              work.numel() * 8, _ffi.stream_handle(xb.device))
+    return out
+
+
+@dataclasses.dataclass
+class LstsqResult:
+    x: torch.Tensor     # (k, n) least-squares solutions
+    iters: int          # refinement steps
+    step: list          # last max|dx| / max|x| per right-hand side
+    converged: bool
+
+
+def qr_lstsq(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, max_iter: int = 10,
+             factor: QR32 | None = None, split: SplitMatrix | None = None,
+             split_t: SplitMatrix | None = None) -> LstsqResult:
+    """min ||b - A x||_2 for a tall full-rank A by corrected semi-normal
+    equations: R from the TF32 QR (qr_factor_tf32), then
+        x += R^{-1} R^{-T} Aᵀ (b - A x)
+    with b - A x and Aᵀ r in double-float arithmetic (A and Aᵀ held as FP32
+    hi + lo pairs) and the two triangular solves in FP64 (lxgb_trsm_f64), until
+    max|dx| <= tol max|x|.  Each step contracts the error by about
+    kappa(A)^2 u_TF32, so well-conditioned problems reach FP64 accuracy in a
+    few steps (Björck's CSNE; no Q is applied)."""
+    a64 = as_device_f64(a).contiguous()
+    m, n = a64.shape
+    b64 = as_device_f64(b)
+    if b64.ndim == 1:
+        b64 = b64.reshape(1, -1)
+    b64 = b64.contiguous()
+    k = b64.shape[0]
+    if factor is None:
+        factor = qr_factor_tf32(a64)
+    if split is None:
+        split = split_matrix(a64)
+    if split_t is None:
+        split_t = split_matrix(a64.T.contiguous())
+    from . import _dense
+
+    x = torch.zeros((k, n), dtype=torch.float64, device=a64.device)
+    r = b64.clone()
+    steps, it, converged = [float("inf")] * k, 0, False
+    for it in range(1, max_iter + 1):
+        g = _gemv_df(split_t, r, None)                                     # Aᵀ r
+        y = _dense.trsv(factor.rt, g, lower=True, trans=False, unit=False)  # Rᵀ y = g
+        d = _dense.trsv(factor.rt, y, lower=True, trans=True, unit=False)   # R d = y
+        x += d
+        r = _gemv_df(split, x, b64)                                        # b - A x
+        dn = d.abs().amax(dim=1)
+        xn = x.abs().amax(dim=1)
+        steps = (dn / torch.clamp(xn, min=1e-300)).cpu().tolist()
+        if all(s_ <= tol for s_ in steps):
+            converged = True
+            break
+    return LstsqResult(x, it, steps, converged)
+
