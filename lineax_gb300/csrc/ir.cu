@@ -263,6 +263,71 @@ gemv16_kernel(int m, int ncol, const float* __restrict__ Mh, const float* __rest
   }
 }
 
+// Few right-hand sides (k <= 4): one warp per matrix row, lanes along the
+// columns, k double-float accumulators per lane reduced across the warp.
+// The matrix streams from HBM once; x (hi/lo, k × n) is shared through L1/L2.
+template <int K, bool LO, int OUT>
+__global__ void __launch_bounds__(256)
+gemv_rows_df_kernel(int m, int ncol, const float* __restrict__ Mh, const float* __restrict__ Ml,
+                    int64_t ldm, const float* __restrict__ xh, const float* __restrict__ xl,
+                    int64_t ldx, double* __restrict__ y64, const double* __restrict__ b64,
+                    int64_t ldy) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= m) return;  // whole warps
+  const float* mr = Mh + (int64_t)row * ldm;
+  const float* ml = LO ? Ml + (int64_t)row * ldm : mr;
+  float sh[K], sl[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) sh[q] = sl[q] = 0.0f;
+  for (int c = lane; c < ncol; c += 32) {
+    const float a = __ldg(mr + c);
+    const float al = LO ? __ldg(ml + c) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const float x = __ldg(xh + (int64_t)q * ldx + c);
+      const float xlv = __ldg(xl + (int64_t)q * ldx + c);
+      const float p = a * x;
+      float e = fmaf(a, x, -p);
+      e = fmaf(a, xlv, e);
+      if (LO) e = fmaf(al, x, e);
+      float err;
+      two_sum(sh[q], p, err);
+      sl[q] += err + e;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const float oh = __shfl_xor_sync(0xffffffffu, sh[q], off);
+      const float ol = __shfl_xor_sync(0xffffffffu, sl[q], off);
+      float err;
+      two_sum(sh[q], oh, err);
+      sl[q] += ol + err;
+    }
+  if (lane < K) {
+    float oh = sh[0], ol = sl[0];
+#pragma unroll
+    for (int q = 1; q < K; ++q)
+      if (lane == q) { oh = sh[q]; ol = sl[q]; }
+    const double v = (double)oh + (double)ol;
+    const int64_t o = (int64_t)lane * ldy + row;
+    y64[o] = (OUT == 2) ? b64[o] - v : v;
+  }
+}
+
+template <int K, bool LO>
+static void launch_rows_df(int m, int n, const float* ah, const float* al, int64_t lda,
+                           const float* xh, const float* xl, int64_t ldx, double* y,
+                           const double* b, int64_t ldy, cudaStream_t st) {
+  const unsigned g = (unsigned)((m + 7) / 8);
+  if (b)
+    gemv_rows_df_kernel<K, LO, 2><<<g, 256, 0, st>>>(m, n, ah, al, lda, xh, xl, ldx, y, b, ldy);
+  else
+    gemv_rows_df_kernel<K, LO, 1><<<g, 256, 0, st>>>(m, n, ah, al, lda, xh, xl, ldx, y, b, ldy);
+}
+
 // zh/zl[q][i] = x[q][perm ? perm[i] : i] as a hi + lo pair (zl null: FP32 rounding).
 __global__ void split_rows_kernel(int k, int n, const double* __restrict__ x, int64_t ldx,
                                   const int32_t* __restrict__ perm, float* __restrict__ zh,
@@ -496,6 +561,20 @@ extern "C" int lxgb_gemv_df(int32_t m, int32_t n, const float* a_hi, const float
     split_rows_kernel<<<g, 256, 0, st>>>(nrhs, n, x, ldx, nullptr, xh, mode ? xl : nullptr, nn);
   }
   const bool res = b != nullptr;
+  if (mode == 1 && nrhs <= 4 && n > 0) {
+    // few right-hand sides: one warp per row (the 16 × 16 tiles would idle)
+    switch (nrhs * 2 + (a_lo ? 1 : 0)) {
+      case 2: launch_rows_df<1, false>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 3: launch_rows_df<1, true>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 4: launch_rows_df<2, false>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 5: launch_rows_df<2, true>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 6: launch_rows_df<3, false>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 7: launch_rows_df<3, true>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      case 8: launch_rows_df<4, false>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+      default: launch_rows_df<4, true>(m, n, a_hi, a_lo, lda, xh, xl, nn, y, b, ldy, st); break;
+    }
+    return check_launch("gemv_df");
+  }
   if (mode == 0)
     return res ? launch_gemv16<0, 0, 2>(m, n, a_hi, nullptr, lda, nrhs, xh, nullptr, nn, nullptr,
                                         nullptr, y, b, ldy, st)

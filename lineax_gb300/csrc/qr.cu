@@ -213,7 +213,21 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
       if (tk != T(0)) {
         const T* __restrict__ vk = hk;
         const T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
-        for (int64_t i = i_lo + lane; i < r_hi; i += 32) acc = fma(vk[i], aq[i], acc);
+        // eight independent loads in flight per lane (the rows sit in L2)
+        int64_t i = i_lo + lane;
+        T a8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a8[u] = T(0);
+        for (; i + 7 * 32 < r_hi; i += 8 * 32) {
+          T vv[8], qq[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) { vv[u] = vk[i + 32 * u]; qq[u] = aq[i + 32 * u]; }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) a8[u] = fma(vv[u], qq[u], a8[u]);
+        }
+        for (; i < r_hi; i += 32) a8[0] = fma(vk[i], aq[i], a8[0]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += a8[u];
         acc = warp_sum(acc);
         if (own_k && lane == 0) acc += aq[k];
       }
@@ -228,7 +242,15 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
         const T* __restrict__ vk = hk;
         T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
         if (own_k && lane == 0) aq[k] -= tw;
-        for (int64_t i = i_lo + lane; i < r_hi; i += 32) aq[i] = fma(-tw, vk[i], aq[i]);
+        int64_t i = i_lo + lane;
+        for (; i + 7 * 32 < r_hi; i += 8 * 32) {
+          T vv[8], qq[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) { vv[u] = vk[i + 32 * u]; qq[u] = aq[i + 32 * u]; }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) aq[i + 32 * u] = fma(-tw, vv[u], qq[u]);
+        }
+        for (; i < r_hi; i += 32) aq[i] = fma(-tw, vk[i], aq[i]);
       }
     }
     __syncthreads();

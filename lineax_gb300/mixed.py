@@ -381,7 +381,8 @@ class QR32:
     h: torch.Tensor     # n × m FP32, jnp.linalg.qr(mode="raw") layout (h = Aᵀ factored)
     tau: torch.Tensor   # n FP32
     t: torch.Tensor     # compact-WY T of each 32-column panel
-    rt: torch.Tensor    # Rᵀ (n × n, lower, FP64) for the FP64 triangular solves
+    rt: torch.Tensor    # Rᵀ (n × n, lower, FP64)
+    rinv: InverseLU32 | None  # R^{-T} (linv, lower), R^{-1} (uinv, upper); None if n % 4
 
 
 def qr_factor_tf32(a: torch.Tensor) -> QR32:
@@ -404,7 +405,15 @@ def qr_factor_tf32(a: torch.Tensor) -> QR32:
     if int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the QR update")
     rt = h[:, :n].double().contiguous()
-    return QR32(h, tau, t, rt)
+    # R^{-1} through the LU inversion machinery: R in the upper triangle of a
+    # square FP32 array with identity pivots (its lower triangle is ignored)
+    if n % 4:
+        return QR32(h, tau, t, rt, None)  # 16-byte TMA rows: FP64 triangular solves instead
+    r_sq = h[:, :n].t().contiguous()
+    piv = torch.arange(n, dtype=torch.int32, device=dev)
+    inv = lu_inverse(LU32(r_sq, piv, torch.zeros(1, dtype=torch.int32, device=dev)), "3xtf32")
+    inv = InverseLU32(inv.uinv.t().contiguous(), inv.uinv, inv.perm)
+    return QR32(h, tau, t, rt, inv)
 
 
 def _gemv_df(split: SplitMatrix, x: torch.Tensor, b: torch.Tensor | None) -> torch.Tensor:
@@ -437,7 +446,8 @@ def qr_lstsq(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, max_iter: 
     equations: R from the TF32 QR (qr_factor_tf32), then
         x += R^{-1} R^{-T} Aᵀ (b - A x)
     with b - A x and Aᵀ r in double-float arithmetic (A and Aᵀ held as FP32
-    hi + lo pairs) and the two triangular solves in FP64 (lxgb_trsm_f64), until
+    hi + lo pairs) and R^{-1} R^{-T} applied as two double-float triangular
+    products with the tensor-core inverse of R (lxgb_lu32_inverse), until
     max|dx| <= tol max|x|.  Each step contracts the error by about
     kappa(A)^2 u_TF32, so well-conditioned problems reach FP64 accuracy in a
     few steps (Björck's CSNE; no Q is applied)."""
@@ -454,15 +464,20 @@ def qr_lstsq(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, max_iter: 
         split = split_matrix(a64)
     if split_t is None:
         split_t = split_matrix(a64.T.contiguous())
-    from . import _dense
-
     x = torch.zeros((k, n), dtype=torch.float64, device=a64.device)
     r = b64.clone()
+    rinv = (InverseLUPreconditioner(None, factor.rinv, "df")  # d = R^{-1} (R^{-T} g)
+            if factor.rinv is not None else None)
     steps, it, converged = [float("inf")] * k, 0, False
     for it in range(1, max_iter + 1):
         g = _gemv_df(split_t, r, None)                                     # Aᵀ r
-        y = _dense.trsv(factor.rt, g, lower=True, trans=False, unit=False)  # Rᵀ y = g
-        d = _dense.trsv(factor.rt, y, lower=True, trans=True, unit=False)   # R d = y
+        if rinv is not None:
+            d = rinv.mv_block(g)
+        else:
+            from . import _dense
+
+            y = _dense.trsv(factor.rt, g, lower=True, trans=False, unit=False)  # Rᵀ y = g
+            d = _dense.trsv(factor.rt, y, lower=True, trans=True, unit=False)   # R d = y
         x += d
         r = _gemv_df(split, x, b64)                                        # b - A x
         dn = d.abs().amax(dim=1)

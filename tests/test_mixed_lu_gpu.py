@@ -93,7 +93,8 @@ def test_inverse_preconditioner_apply(dev, n, k, arith, bound):
     assert np.max(np.abs(y - ref) / scale) < bound
 
 
-@pytest.mark.parametrize("m,n,k", [(300, 200, 5), (512, 512, 16), (129, 700, 20)])
+@pytest.mark.parametrize("m,n,k", [(300, 200, 5), (512, 512, 16), (129, 700, 20), (333, 800, 1),
+                                   (200, 1000, 3), (64, 2048, 4)])
 def test_double_float_gemv(dev, m, n, k):
     """A x and b - A x with A as an FP32 hi + lo pair: FP64-level accuracy in
     double-float, FP32-level on the hi part alone."""

@@ -89,7 +89,7 @@ def test_reference_kat_qr(dev, name):
     np.testing.assert_allclose(sol.value.cpu().numpy(), k["solution"], rtol=1e-14)
 
 
-@pytest.mark.parametrize("m,n,k", [(4096, 512, 1), (2048, 300, 3), (1024, 256, 2)])
+@pytest.mark.parametrize("m,n,k", [(4096, 512, 1), (2048, 300, 3), (1024, 256, 2), (1024, 130, 1)])
 def test_mixed_precision_least_squares(dev, m, n, k):
     """TF32 tensor-core QR + corrected semi-normal equations: the FP64
     least-squares solution (Gaussian tall matrices, kappa ~ 2-3; the
