@@ -179,22 +179,25 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
     block_sums<1>(ss, red, &p_ss[par]);
     if (tid == 0 && own_k) p_alpha[par] = hk[k];
     cluster.sync();
-    if (tid == 0) {
-      T xnorm2 = T(0);
-      for (int c = 0; c < ncta; ++c) xnorm2 += *cluster.map_shared_rank(&p_ss[par], c);
+    if (tid < 32) {
+      // lane c reads CTA c's partial (parallel remote loads), fixed-order tree
+      T xnorm2 = (tid < ncta) ? *cluster.map_shared_rank(&p_ss[par], tid) : T(0);
+      xnorm2 = warp_sum(xnorm2);
       const int own = (int)((k - j0) / rows_per_cta);
       const T alpha = *cluster.map_shared_rank(&p_alpha[par], own);
-      const T xnorm = sqrt(xnorm2);
-      if (xnorm == T(0)) {
-        s_tau = T(0);
-        s_scal = T(1);
-      } else {
-        const T beta = -copysign(hypot(alpha, xnorm), alpha);
-        s_tau = (beta - alpha) / beta;
-        s_scal = T(1) / (alpha - beta);
-        if (own_k) hk[k] = beta;
+      if (tid == 0) {
+        const T xnorm = sqrt(xnorm2);
+        if (xnorm == T(0)) {
+          s_tau = T(0);
+          s_scal = T(1);
+        } else {
+          const T beta = -copysign(hypot(alpha, xnorm), alpha);
+          s_tau = (beta - alpha) / beta;
+          s_scal = T(1) / (alpha - beta);
+          if (own_k) hk[k] = beta;
+        }
+        if (rank == 0) tau[k] = s_tau;
       }
-      if (rank == 0) tau[k] = s_tau;
     }
     __syncthreads();
     const T tk = s_tau;
@@ -236,8 +239,8 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
     cluster.sync();
     if (tk != T(0) && nrem > 0) {
       for (int q = warp; q < nrem; q += nwarps) {
-        T w = T(0);
-        for (int c = 0; c < ncta; ++c) w += cluster.map_shared_rank(&p_w[par][0], c)[q];
+        T w = (lane < ncta) ? cluster.map_shared_rank(&p_w[par][0], lane)[q] : T(0);
+        w = warp_sum(w);
         const T tw = tk * w;
         const T* __restrict__ vk = hk;
         T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;

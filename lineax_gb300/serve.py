@@ -23,9 +23,16 @@ route:
                LU when refinement stalls); the factor stays resident for later
                requests on the operator.
 
+Serving is continuous: run() keeps admitting requests as they arrive and as
+memory frees up while earlier work is still on the GPU.  Admitted work goes
+to a pool of worker threads, each with its own CUDA stream (a ragged
+Cholesky group or a small-LU group is one job, each large request is one
+job), so requests overlap on the device; a job's device memory is released
+back to the admission budget when it completes.
+
 mode="fp64" serves the same requests with the plain FP64 GPU path of this
-library (ragged FP64 Cholesky, FP64 LU): the denominator of the mixed
-path's speed-up.  A square QR request is served by LU in both modes: for a
+library (ragged FP64 Cholesky, FP64 LU) on one stream: the denominator of
+the mixed path's speed-up.  A square QR request is served by LU in both modes: for a
 nonsingular square A both define the same solution, and lineax's own
 AutoLinearSolver picks LU for square operators (lineax/_solve.py:555-600).
 Every completion carries its normwise backward error; a request's result
@@ -35,7 +42,9 @@ does not depend on what else was in its batch.
 from __future__ import annotations
 
 import collections
+import concurrent.futures
 import dataclasses
+import threading
 import time
 
 import torch
@@ -122,7 +131,9 @@ class Scheduler:
         self.queue: collections.deque = collections.deque()
         self.resident: collections.OrderedDict = collections.OrderedDict()
         self.resident_total = 0
+        self.inflight = 0          # bytes held by admitted, unfinished requests
         self.rejected: list = []
+        self.lock = threading.RLock()
 
     def submit(self, req: Request) -> None:
         self.queue.append(req)
@@ -135,7 +146,7 @@ class Scheduler:
 
     def _evict_for(self, need: int, pinned: set) -> None:
         for op_id in list(self.resident):
-            if self.resident_total + need <= self.budget:
+            if self.resident_total + self.inflight + need <= self.budget:
                 return
             if op_id in pinned:
                 continue
@@ -143,39 +154,53 @@ class Scheduler:
             self.resident_total -= nbytes
 
     def admit(self, now: float) -> list:
-        """Requests that have arrived by `now`, in order, while they fit."""
-        batch, used, pinned = [], 0, set()
-        while self.queue and self.queue[0].arrival <= now:
-            req = self.queue[0]
-            route = route_of(req.kind, req.n, self.mode)
-            need = footprint(route, req.n, req.nrhs)
-            if req.op_id in self.resident:  # its resident part is already charged
-                need = max(need - self.resident[req.op_id][0], 0)
-            self._evict_for(used + need, pinned | {req.op_id})
-            if self.resident_total + used + need > self.budget:
-                if not batch and need > self.budget:
-                    self.rejected.append(self.queue.popleft())  # can never fit
-                    continue
-                break
-            batch.append(self.queue.popleft())
-            used += need
-            pinned.add(req.op_id)
-        return batch
+        """Requests that have arrived by `now`, in order, while they fit
+        beside the resident operators and the work still in flight; their
+        footprints stay charged until release()."""
+        with self.lock:
+            batch, used, pinned = [], 0, set()
+            while self.queue and self.queue[0].arrival <= now:
+                req = self.queue[0]
+                route = route_of(req.kind, req.n, self.mode)
+                need = footprint(route, req.n, req.nrhs)
+                if req.op_id in self.resident:  # its resident part is already charged
+                    need = max(need - self.resident[req.op_id][0], 0)
+                self._evict_for(used + need, pinned | {req.op_id})
+                if self.resident_total + self.inflight + used + need > self.budget:
+                    if not batch and self.inflight == 0 and need > self.budget:
+                        self.rejected.append(self.queue.popleft())  # can never fit
+                        continue
+                    break
+                batch.append(self.queue.popleft())
+                req._charge = need
+                used += need
+                pinned.add(req.op_id)
+            self.inflight += used
+            return batch
+
+    def release(self, reqs) -> None:
+        """Return the footprints of finished requests to the budget."""
+        with self.lock:
+            for r in reqs:
+                self.inflight -= getattr(r, "_charge", 0)
+                r._charge = 0
 
     def lookup(self, op_id):
-        hit = self.resident.get(op_id)
-        if hit is None:
-            return None
-        self.resident.move_to_end(op_id)
-        return hit[1]
+        with self.lock:
+            hit = self.resident.get(op_id)
+            if hit is None:
+                return None
+            self.resident.move_to_end(op_id)
+            return hit[1]
 
     def remember(self, op_id, nbytes: int, payload) -> None:
-        if op_id in self.resident:
-            self.resident_total -= self.resident.pop(op_id)[0]
-        self._evict_for(nbytes, {op_id})
-        if self.resident_total + nbytes <= self.budget:
-            self.resident[op_id] = (int(nbytes), payload)
-            self.resident_total += int(nbytes)
+        with self.lock:
+            if op_id in self.resident:
+                self.resident_total -= self.resident.pop(op_id)[0]
+            self._evict_for(nbytes, {op_id})
+            if self.resident_total + self.inflight + nbytes <= self.budget:
+                self.resident[op_id] = (int(nbytes), payload)
+                self.resident_total += int(nbytes)
 
 
 def _pad_identity(a: torch.Tensor, n_to: int) -> torch.Tensor:
@@ -217,16 +242,19 @@ class SolveServer:
     """Serve Requests on one GPU (see the module docstring)."""
 
     def __init__(self, device="cuda", mode: str = "mixed", hbm_budget: int = 64 << 30,
-                 tol: float = 1e-12, precision: str = "3xtf32"):
+                 tol: float = 1e-12, precision: str = "3xtf32", streams: int | None = None):
         if mode not in ("mixed", "fp64"):
             raise ValueError("mode must be 'mixed' or 'fp64'")
         self.device = torch.device(device)
+        if self.device.index is None:
+            self.device = torch.device(self.device.type, torch.cuda.current_device())
         self.mode = mode
         self.tol = tol
         self.precision = precision
+        self.streams = streams if streams is not None else (4 if mode == "mixed" else 1)
         self.sched = Scheduler(hbm_budget, mode)
         self.registry: dict = {}  # op_id -> host FP64 matrix (the client's copy)
-        self._ws = None
+        self._tls = threading.local()  # per worker thread: its stream and workspace
 
     def register(self, op_id, a_host: torch.Tensor) -> None:
         self.registry[op_id] = a_host
@@ -253,9 +281,11 @@ class SolveServer:
         rb = batched.RaggedBatch.from_lists(mats, rhs, device=self.device)
         out = []
         if self.mode == "mixed":
-            if self._ws is None or not self._ws.fits(rb.batch, rb.max_n, rb.max_nrhs):
-                self._ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, self.device)
-            res = batched.spd_solve_ragged_mixed(rb, tol=self.tol, workspace=self._ws)
+            ws = getattr(self._tls, "ws", None)
+            if ws is None or not ws.fits(rb.batch, rb.max_n, rb.max_nrhs):
+                ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, self.device)
+                self._tls.ws = ws
+            res = batched.spd_solve_ragged_mixed(rb, tol=self.tol, workspace=ws)
             info = res.info.cpu().tolist()
             berr = res.berr.cpu().tolist()
             for s, req in enumerate(reqs):
@@ -352,30 +382,77 @@ class SolveServer:
         torch.cuda.synchronize(self.device)
         return out
 
+    def _jobs(self, batch: list) -> list:
+        """Admitted requests as jobs: one per ragged Cholesky group, one per
+        small-LU group, one per large request."""
+        groups = collections.defaultdict(list)
+        for r in batch:
+            groups[route_of(r.kind, r.n, self.mode)].append(r)
+        jobs = []
+        if groups["chol_ragged"]:
+            jobs.append((self._run_chol, groups["chol_ragged"]))
+        if groups["lu_small"]:
+            jobs.append((self._run_small, groups["lu_small"]))
+        for r in groups["lu_mixed"]:
+            jobs.append((lambda rs: [self._run_mixed(rs[0])], [r]))
+        for r in groups["lu_f64"]:
+            jobs.append((lambda rs: [self._run_f64(rs[0])], [r]))
+        return jobs
+
+    def _work(self, fn, reqs, t0: float):
+        """One job on this worker thread's stream; returns its completions
+        stamped with the time the device finished them."""
+        st = getattr(self._tls, "stream", None)
+        if st is None:
+            st = torch.cuda.Stream(self.device)
+            self._tls.stream = st
+        with torch.cuda.device(self.device), torch.cuda.stream(st):
+            out = fn(reqs)
+            st.synchronize()
+        t = time.perf_counter() - t0
+        for c in out:
+            c.finished = t
+        return out
+
     def run(self, requests: list, realtime: bool = True) -> list:
         """Serve requests whose `arrival` times are seconds after the start
-        (open loop: arrivals do not wait for completions).  Returns the
-        completions in request-id order with finish times and latencies."""
+        (open loop: arrivals do not wait for completions).  Admission keeps
+        running while admitted work is on the GPU; jobs run on `streams`
+        worker threads with one CUDA stream each.  Returns the completions in
+        request-id order with finish times and latencies."""
         for r in sorted(requests, key=lambda q: q.arrival):
             self.sched.submit(r)
         arrival = {r.rid: r.arrival for r in requests}
         done = {}
         t0 = time.perf_counter()
-        while self.sched.pending():
-            now = time.perf_counter() - t0 if realtime else float("inf")
-            batch = self.sched.admit(now)
-            if not batch:
-                nxt = self.sched.next_arrival()
-                if nxt is not None and nxt > now:
-                    time.sleep(min(nxt - now, 0.01))
+        inflight = {}
+        with concurrent.futures.ThreadPoolExecutor(max_workers=self.streams) as pool:
+            while self.sched.pending() or inflight:
+                now = time.perf_counter() - t0 if realtime else float("inf")
+                batch = self.sched.admit(now) if self.sched.pending() else []
+                for fn, reqs in self._jobs(batch):
+                    inflight[pool.submit(self._work, fn, reqs, t0)] = reqs
+                if batch:
                     continue
-                if not self.sched.pending():
-                    break
-                raise MemoryError("a request does not fit the HBM budget")
-            for c in self.execute(batch):
-                c.finished = time.perf_counter() - t0
-                c.latency = c.finished - arrival[c.rid]
-                done[c.rid] = c
+                if not inflight:
+                    nxt = self.sched.next_arrival()
+                    if nxt is None:
+                        break
+                    if nxt > now:
+                        time.sleep(min(nxt - now, 0.002))
+                        continue
+                    raise MemoryError("a request does not fit the HBM budget")
+                nxt = self.sched.next_arrival()
+                timeout = None if nxt is None else max(0.0, min(nxt - now, 0.002))
+                finished, _ = concurrent.futures.wait(
+                    list(inflight), timeout=timeout,
+                    return_when=concurrent.futures.FIRST_COMPLETED)
+                for f in finished:
+                    reqs = inflight.pop(f)
+                    self.sched.release(reqs)
+                    for c in f.result():
+                        c.latency = c.finished - arrival[c.rid]
+                        done[c.rid] = c
         return [done[k] for k in sorted(done)]
 
 

@@ -30,10 +30,14 @@ def test_admission_is_fifo_and_respects_arrival_and_budget():
         s.submit(r)
     first = s.admit(now=1.0)
     assert [r.rid for r in first] == [0, 1]          # the third does not fit beside them
+    assert s.admit(now=1.0) == []                    # still in flight: no room
+    s.release(first)                                 # they finished
     second = s.admit(now=1.0)
     assert [r.rid for r in second] == [2]            # request 3 has not arrived yet
     assert s.admit(now=1.0) == [] and s.next_arrival() == 5.0
-    assert [r.rid for r in s.admit(now=5.0)] == [3]
+    assert [r.rid for r in s.admit(now=5.0)] == [3]  # small: fits beside request 2
+    s.release(second)
+    assert s.inflight > 0                             # request 3 still charged
 
 
 def test_residents_are_charged_and_evicted_lru():
