@@ -250,11 +250,13 @@ def run_gpu(args):
     b_host = torch.from_numpy(wl.b).pin_memory()
     rb = batched.RaggedBatch.from_packed(a_host.to(dev), b_host.to(dev), wl.n, wl.nrhs, dev)
     ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, dev)
-    out = batched.spd_solve_ragged_mixed(rb, TOL, workspace=ws)
+    # one persistent launch per step, replayed from a captured CUDA graph
+    graphed = batched.CapturedMixedSolve(rb, TOL, workspace=ws)
+    out = graphed.out
     stream = torch.cuda.current_stream(dev)
 
     def step():
-        batched.spd_solve_ragged_mixed(rb, TOL, workspace=ws, out=out)
+        graphed.replay()
 
     for _ in range(args.warmup):
         step()
@@ -371,6 +373,8 @@ def run_gpu(args):
             "nrhs": "1..8", "A": "G G^T/n + 1e-2 I", "tol": TOL,
             "l2": "inputs larger than L2 (%.2f GB of matrices per step)" % (8 * (ns * ns).sum() / 1e9),
             "parallelism": f"replicas x{world}",
+            "launch": "one persistent posv_mixed_kernel launch per step, replayed from a "
+                      "captured CUDA graph",
         },
         "latency_ms": {"p50": _pct(per_step, 50), "p99": _pct(per_step, 99)},
         "correct": {"all_berr_le_tol": ok, "max_berr": float(berr.max()),
@@ -719,17 +723,19 @@ def run_serve(args):
         return v[min(len(v) - 1, int(round(p / 100.0 * (len(v) - 1))))]
 
     def one(mode, rate, seed):
-        reqs = serve.synthetic_requests(count, seed=seed, nmax=args.serve_nmax, rate=rate)
+        reqs = serve.synthetic_requests(count, seed=seed, nmax=args.serve_nmax, rate=rate,
+                                        device=dev)
         for r in reqs:
             if r.a is not None:
                 r.a = r.a.pin_memory()
             r.b = r.b.pin_memory()
+        torch.cuda.synchronize()
         srv = serve.SolveServer(dev, mode=mode, hbm_budget=int(args.serve_budget_gb * 2**30))
         t0 = time.perf_counter()
         out = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         lat = [c.latency * 1e3 for c in out]
-        return {"mode": mode, "offered_rate": rate, "requests": len(out),
+        return {"mode": mode, "streams": srv.streams, "offered_rate": rate, "requests": len(out),
                 "solves_per_s": len(out) / wall,
                 "rhs_per_s": sum(r.nrhs for r in reqs) / wall, "wall_s": wall,
                 "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
@@ -742,17 +748,19 @@ def run_serve(args):
     for mode in ("mixed", "fp64"):
         serve.SolveServer(dev, mode=mode).run(warm, realtime=False)
     torch.cuda.synchronize()
+    tag = f"serve_{count}req_n32-{args.serve_nmax}"
     sat = {m: one(m, None, 5) for m in ("fp64", "mixed")}
     for m in ("fp64", "mixed"):
-        print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
-                          "saturation", **sat[m]}), flush=True)
-    rate = 0.5 * sat["fp64"]["solves_per_s"]
+        print(json.dumps({"workload": tag, "phase": "saturation", **sat[m]}), flush=True)
+    print(json.dumps({"workload": tag, "phase": "speedup",
+                      "mixed_over_fp64_solves_per_s":
+                          sat["mixed"]["solves_per_s"] / sat["fp64"]["solves_per_s"]}),
+          flush=True)
+    # open-loop rate sweep: fractions of each server's saturation throughput
     for m in ("fp64", "mixed"):
-        print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
-                          "open_loop", **one(m, rate, 6)}), flush=True)
-    rate = 0.5 * sat["mixed"]["solves_per_s"]
-    print(json.dumps({"workload": f"serve_{count}req_n32-{args.serve_nmax}", "phase":
-                      "open_loop", **one("mixed", rate, 6)}), flush=True)
+        for frac in (0.25, 0.5, 0.75):
+            print(json.dumps({"workload": tag, "phase": "open_loop", "load": frac,
+                              **one(m, frac * sat[m]["solves_per_s"], 6)}), flush=True)
 
 
 def run_peaks(args):

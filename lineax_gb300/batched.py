@@ -174,6 +174,31 @@ def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int
     return out
 
 
+class CapturedMixedSolve:
+    """The mixed-precision ragged solve (queue reset + one persistent
+    posv_mixed_kernel launch) captured once in a CUDA graph for a fixed batch,
+    workspace and output, then replayed: repeated solves of a resident batch
+    cost one graph launch.  The library holds no state between calls, so the
+    captured launch reads whatever the batch's buffers hold at replay time."""
+
+    def __init__(self, batch: RaggedBatch, tol: float = 1e-12, max_iter: int = 10,
+                 workspace: MixedWorkspace | None = None, out: MixedResult | None = None):
+        dev = batch.a.device
+        if workspace is None:
+            workspace = MixedWorkspace(batch.batch, batch.max_n, batch.max_nrhs, dev)
+        self.batch, self.workspace = batch, workspace
+        # first call outside the capture: sets the kernel's shared-memory limit
+        self.out = spd_solve_ragged_mixed(batch, tol, max_iter, workspace, out)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            spd_solve_ragged_mixed(batch, tol, max_iter, workspace, self.out)
+
+    def replay(self) -> MixedResult:
+        self.graph.replay()
+        return self.out
+
+
 class HostRaggedSPDSolver:
     """Solve ragged SPD batches whose data lives in host memory.
 

@@ -457,13 +457,16 @@ class SolveServer:
 
 
 def synthetic_requests(count: int, seed: int = 0, nmin: int = 32, nmax: int = 4096,
-                       reuse: float = 0.3, rate: float | None = None, mix=(0.5, 0.3, 0.2)):
+                       reuse: float = 0.3, rate: float | None = None, mix=(0.5, 0.3, 0.2),
+                       device=None):
     """The serving mix: kinds LU/Cholesky/QR with probabilities `mix`, n
     log-uniform on [nmin, nmax], 1-16 right-hand sides, a fraction `reuse`
     of requests on an operator seen before (no matrix sent), Poisson arrivals
-    at `rate` per second (all at t = 0 when rate is None).  Host tensors;
-    Cholesky operators are SPD ((G + Gᵀ)/sqrt(2n) + 3I, spectrum in [1, 5]),
-    the others G/sqrt(n) + I."""
+    at `rate` per second (all at t = 0 when rate is None).  Matrices as in the
+    single-workload benchmarks: Cholesky operators G Gᵀ/n + 1e-2 I (the ragged
+    SPD workload), the others G/sqrt(n) + I (the batched-LU workload), with G
+    i.i.d. N(0,1) from a per-operator seed.  Built on `device` when given (the
+    G Gᵀ products of large orders), returned as host tensors."""
     import numpy as np
 
     rng = np.random.default_rng([seed, 0x5E7])
@@ -478,12 +481,12 @@ def synthetic_requests(count: int, seed: int = 0, nmin: int = 32, nmax: int = 40
             kind = KINDS[int(rng.choice(3, p=list(mix)))]
             n = int(np.clip(np.floor(np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1)))),
                             nmin, nmax))
-            g = torch.from_numpy(rng.standard_normal((n, n)))
-            eye = torch.eye(n, dtype=torch.float64)
-            # SPD: the symmetric part scaled to spectrum [-2, 2], shifted by 3
-            a = ((g + g.T) / np.sqrt(2.0 * n) + 3.0 * eye) if kind == "cholesky" else \
-                (g / np.sqrt(n) + eye)
             op_id = len(ops)
+            gen = torch.Generator(device=device or "cpu").manual_seed(seed * 1_000_003 + op_id)
+            g = torch.randn(n, n, dtype=torch.float64, device=device or "cpu", generator=gen)
+            eye = torch.eye(n, dtype=torch.float64, device=g.device)
+            a = (g @ g.T / n + 1e-2 * eye) if kind == "cholesky" else (g / np.sqrt(n) + eye)
+            a = a.cpu()
             ops.append((op_id, kind, n))
         k = int(rng.integers(1, 17))
         b = torch.from_numpy(rng.standard_normal((k, n)))
