@@ -476,6 +476,17 @@ def run_gmres_ir(args):
             emit({"case": "fp64_lu", "cond": cond, "factor_ms": e0.elapsed_time(e1),
                   "solve_ms": e1.elapsed_time(e2), "total_ms": e0.elapsed_time(e2),
                   "max_berr": berr, "solves_per_s": k / (e0.elapsed_time(e2) * 1e-3)})
+            if not args.no_cpu:
+                import scipy.linalg as sl
+
+                ah, bh = a.cpu().numpy(), b.cpu().numpy()
+                cpu_s, reps = _cpu_time(lambda: sl.lu_solve(sl.lu_factor(ah), bh.T),
+                                        min_seconds=1.0, max_reps=3)
+                emit({"case": "cpu_baseline", "cond": cond, "value": k / cpu_s,
+                      "unit": "solves/s", "cores": _host_cores(), "kind": "port",
+                      "sample": f"SciPy LAPACK lu_factor + lu_solve of the same n={n} "
+                                f"system, 16 right-hand sides, {reps} repetitions",
+                      "ms": cpu_s * 1e3})
             del lu, x
             torch.cuda.empty_cache()
         for prec in args.precisions.split(","):
@@ -512,6 +523,23 @@ def _events(n):
     import torch
 
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def _cpu_time(fn, min_seconds=3.0, max_reps=1000):
+    """Host-core timing of fn (all threads the BLAS uses): repeats until
+    min_seconds have passed; returns (seconds per call, calls)."""
+    fn()  # warm (imports, first touch)
+    t0, reps = time.perf_counter(), 0
+    while True:
+        fn()
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= max_reps:
+            return el / reps, reps
+
+
+def _host_cores():
+    return len(os.sched_getaffinity(0))
 
 
 def _fp64_peak():
@@ -572,6 +600,12 @@ def run_lu_batch(args):
                for i in range(batch))
     lu_ref = [sl.lu_factor(a_h[i]) for i in range(4)]
     flops = batch * (2 / 3 * n ** 3 + 2 * n * n)
+
+    def cpu_step():
+        for i in range(batch):
+            sl.lu_solve(sl.lu_factor(a_h[i]), b_h[i])
+
+    cpu_s, cpu_reps = _cpu_time(cpu_step)
     print(json.dumps({
         "workload": "lu_batch_64x128_f64", "metric": "LU solves/s (factor + solve)",
         "unit": "solves/s", "value": batch / (ms * 1e-3), "ms_per_step": ms,
@@ -584,6 +618,9 @@ def run_lu_batch(args):
         "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12,
                      "peak": _fp64_peak(), "unit": "TFLOP/s",
                      "frac": flops / (ms * 1e-3) / 1e12 / _fp64_peak()},
+        "cpu_baseline": {"value": batch / cpu_s, "unit": "solves/s", "cores": _host_cores(),
+                         "kind": "port", "sample": f"the same 64 systems, SciPy LAPACK "
+                         f"lu_factor + lu_solve, {cpu_reps} repetitions"},
         "steps": args.steps, "warmup": args.warmup}), flush=True)
 
 
@@ -636,6 +673,20 @@ def run_qr_ls(args):
                          {"bound": "tensor (TF32 updates)", "effective_tflops":
                           flops / (ms * 1e-3) / 1e12})}
     out["value"] = out["mixed"]["solves_per_s"]
+    if not args.no_cpu:
+        import scipy.linalg as sl
+
+        ah, bh = a.cpu().numpy(), b.cpu().numpy()
+
+        def cpu_step():
+            q, r = sl.qr(ah, mode="economic")
+            sl.solve_triangular(r, q.T @ bh)
+
+        cpu_s, reps = _cpu_time(cpu_step, min_seconds=2.0, max_reps=3)
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "solves/s", "cores": _host_cores(),
+                               "kind": "port", "sample": f"SciPy LAPACK economic QR + "
+                               f"triangular solve of the same {m}×{n} problem, {reps} "
+                               "repetitions"}
     out["steps"], out["warmup"] = args.steps, args.warmup
     print(json.dumps(out), flush=True)
 
@@ -690,6 +741,32 @@ def run_cg_poisson(args):
                      "roofline": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
                                   "peak": 6784.0, "frac": gbs / 6784.0}}
     out["value"] = out["mixed"]["iterations_per_s"]
+    if not args.no_cpu:
+        import numpy as np
+        import scipy.sparse as sp
+
+        t1 = sp.diags([-np.ones(nx - 1), 2 * np.ones(nx), -np.ones(nx - 1)], [-1, 0, 1])
+        lap = (sp.kron(sp.identity(ny), t1) + sp.kron(t1, sp.identity(nx))).tocsr()
+        kb = min(k, 8)
+        bh = b[:kb].cpu().numpy().T.copy()
+        st = {"x": np.zeros_like(bh), "r": bh.copy(), "p": bh.copy(),
+              "g": (bh * bh).sum(0)}
+
+        def cpu_iter():  # one CG iteration on kb right-hand sides (matvec, dots, axpys)
+            ap = lap @ st["p"]
+            alpha = st["g"] / (st["p"] * ap).sum(0)
+            st["x"] += alpha * st["p"]
+            st["r"] -= alpha * ap
+            gn = (st["r"] * st["r"]).sum(0)
+            st["p"] = st["r"] + (gn / st["g"]) * st["p"]
+            st["g"] = gn
+
+        cpu_s, reps = _cpu_time(cpu_iter, min_seconds=3.0, max_reps=50)
+        out["cpu_baseline"] = {"value": (kb / k) / cpu_s, "unit": "iterations/s (64 RHS)",
+                               "cores": _host_cores(), "kind": "port",
+                               "sample": f"{reps} FP64 CG iterations on {kb} of the 64 "
+                               "right-hand sides with a SciPy CSR 5-point Laplacian, scaled to "
+                               "64"}
     if args.cg_full:
         e0.record()
         res = _krylov.cg_poisson_mixed(op, b, rtol=rtol, atol=atol)
@@ -756,6 +833,29 @@ def run_serve(args):
                       "mixed_over_fp64_solves_per_s":
                           sat["mixed"]["solves_per_s"] / sat["fp64"]["solves_per_s"]}),
           flush=True)
+    if not args.no_cpu:
+        # the same request stream solved one request at a time on the host
+        # cores with SciPy LAPACK (Cholesky for SPD requests, LU otherwise)
+        import scipy.linalg as sl
+
+        reqs = serve.synthetic_requests(60, seed=5, nmax=args.serve_nmax)
+        mats = {r.op_id: r.a.numpy() for r in reqs if r.a is not None}
+
+        def cpu_stream():
+            for r in reqs:
+                a = mats[r.op_id]
+                bb = r.b.numpy().T
+                if r.kind == "cholesky":
+                    sl.cho_solve(sl.cho_factor(a), bb)
+                else:
+                    sl.lu_solve(sl.lu_factor(a), bb)
+
+        cpu_s, reps = _cpu_time(cpu_stream, min_seconds=1.0, max_reps=2)
+        print(json.dumps({"workload": tag, "phase": "cpu_baseline", "value": len(reqs) / cpu_s,
+                          "unit": "solves/s", "cores": _host_cores(), "kind": "port",
+                          "sample": "the first 60 requests of the stream (no resident "
+                                    "factors), SciPy LAPACK, one request at a time"}),
+              flush=True)
     # open-loop rate sweep: fractions of each server's saturation throughput
     for m in ("fp64", "mixed"):
         for frac in (0.25, 0.5, 0.75):
