@@ -152,10 +152,14 @@ __device__ void block_sums(T (&v)[NV], T (*red)[kQrNB], T* out) {
 // Partials are double-buffered by column parity: two barriers per column.
 // Then G = VᵀV from per-CTA partials and T by larft's recurrence in CTA 0.
 // Same rules as qr_panel_kernel + qr_larft_kernel (LAPACK geqr2/larfg/larft).
-template <typename T>
+// SM: the CTA's rows of the panel are staged in dynamic shared memory for the
+// whole panel (32 × rows_per_cta values; the FP32 factor's slices fit) instead
+// of being streamed from L2 column by column.
+template <typename T, bool SM>
 __global__ void __launch_bounds__(kQrCluThreads, 1)
 qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
                         T* __restrict__ h, T* __restrict__ tau, T* __restrict__ t_out) {
+  extern __shared__ __align__(16) unsigned char qr_dyn[];
   __shared__ T red[kQrCluThreads / 32][kQrNB];
   __shared__ T p_ss[2], p_alpha[2];
   __shared__ T p_w[2][kQrNB];
@@ -169,15 +173,25 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
   const int nb = pe - j0;
   const int64_t r_lo = j0 + (int64_t)rank * rows_per_cta;
   const int64_t r_hi = min(mm, r_lo + rows_per_cta);
+  T* S = reinterpret_cast<T*>(qr_dyn);
+  // element i (a global row, r_lo <= i < r_hi) of panel column q
+  auto at = [&](int q, int64_t i) -> T& {
+    return SM ? S[(int64_t)q * rows_per_cta + (i - r_lo)] : h[(int64_t)(j0 + q) * mm + i];
+  };
+  if (SM) {
+    for (int q = 0; q < nb; ++q)
+      for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) at(q, i) = h[(int64_t)(j0 + q) * mm + i];
+    __syncthreads();
+  }
   for (int k = j0; k < pe; ++k) {
     const int par = (k - j0) & 1;
-    T* hk = h + (int64_t)k * mm;
+    const int kk = k - j0;
     const bool own_k = (k >= r_lo && k < r_hi);
     T ss[1] = {T(0)};
     for (int64_t i = max((int64_t)k + 1, r_lo) + tid; i < r_hi; i += blockDim.x)
-      ss[0] = fma(hk[i], hk[i], ss[0]);
+      ss[0] = fma(at(kk, i), at(kk, i), ss[0]);
     block_sums<1>(ss, red, &p_ss[par]);
-    if (tid == 0 && own_k) p_alpha[par] = hk[k];
+    if (tid == 0 && own_k) p_alpha[par] = at(kk, k);
     cluster.sync();
     if (tid < 32) {
       // lane c reads CTA c's partial (parallel remote loads), fixed-order tree
@@ -194,7 +208,7 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
           const T beta = -copysign(hypot(alpha, xnorm), alpha);
           s_tau = (beta - alpha) / beta;
           s_scal = T(1) / (alpha - beta);
-          if (own_k) hk[k] = beta;
+          if (own_k) at(kk, k) = beta;
         }
         if (rank == 0) tau[k] = s_tau;
       }
@@ -206,33 +220,32 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
     const int64_t i_lo = max((int64_t)k + 1, r_lo);
     if (tk != T(0)) {
       const T sc = s_scal;
-      for (int64_t i = i_lo + tid; i < r_hi; i += blockDim.x) hk[i] *= sc;
+      for (int64_t i = i_lo + tid; i < r_hi; i += blockDim.x) at(kk, i) *= sc;
     }
     __syncthreads();
     // one warp per trailing column: w_q partial = v_kᵀ a_q over this CTA's
     // rows (+ a_q[k] from the owner of row k, as v_k[k] = 1)
     for (int q = warp; q < nrem; q += nwarps) {
       T acc = T(0);
+      const int qq = kk + 1 + q;
       if (tk != T(0)) {
-        const T* __restrict__ vk = hk;
-        const T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
-        // eight independent loads in flight per lane (the rows sit in L2)
+        // eight independent loads in flight per lane when the rows sit in L2
         int64_t i = i_lo + lane;
         T a8[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) a8[u] = T(0);
         for (; i + 7 * 32 < r_hi; i += 8 * 32) {
-          T vv[8], qq[8];
+          T vv[8], qv[8];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) { vv[u] = vk[i + 32 * u]; qq[u] = aq[i + 32 * u]; }
+          for (int u = 0; u < 8; ++u) { vv[u] = at(kk, i + 32 * u); qv[u] = at(qq, i + 32 * u); }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) a8[u] = fma(vv[u], qq[u], a8[u]);
+          for (int u = 0; u < 8; ++u) a8[u] = fma(vv[u], qv[u], a8[u]);
         }
-        for (; i < r_hi; i += 32) a8[0] = fma(vk[i], aq[i], a8[0]);
+        for (; i < r_hi; i += 32) a8[0] = fma(at(kk, i), at(qq, i), a8[0]);
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc += a8[u];
         acc = warp_sum(acc);
-        if (own_k && lane == 0) acc += aq[k];
+        if (own_k && lane == 0) acc += at(qq, k);
       }
       if (lane == 0) p_w[par][q] = acc;
     }
@@ -242,18 +255,17 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
         T w = (lane < ncta) ? cluster.map_shared_rank(&p_w[par][0], lane)[q] : T(0);
         w = warp_sum(w);
         const T tw = tk * w;
-        const T* __restrict__ vk = hk;
-        T* __restrict__ aq = h + (int64_t)(k + 1 + q) * mm;
-        if (own_k && lane == 0) aq[k] -= tw;
+        const int qq = kk + 1 + q;
+        if (own_k && lane == 0) at(qq, k) -= tw;
         int64_t i = i_lo + lane;
         for (; i + 7 * 32 < r_hi; i += 8 * 32) {
-          T vv[8], qq[8];
+          T vv[8], qv[8];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) { vv[u] = vk[i + 32 * u]; qq[u] = aq[i + 32 * u]; }
+          for (int u = 0; u < 8; ++u) { vv[u] = at(kk, i + 32 * u); qv[u] = at(qq, i + 32 * u); }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) aq[i + 32 * u] = fma(-tw, vv[u], qq[u]);
+          for (int u = 0; u < 8; ++u) at(qq, i + 32 * u) = fma(-tw, vv[u], qv[u]);
         }
-        for (; i < r_hi; i += 32) aq[i] = fma(-tw, vk[i], aq[i]);
+        for (; i < r_hi; i += 32) at(qq, i) = fma(-tw, at(kk, i), at(qq, i));
       }
     }
     __syncthreads();
@@ -273,7 +285,9 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
       for (int e = tid; e < 64 * kQrNB; e += blockDim.x) {
         const int q = e / 64, ii = e % 64;
         const int64_t i = i0 + ii;
-        Vc[ii][q] = (q < nb && i < r_hi) ? refl(h, mm, j0 + q, i) : T(0);
+        Vc[ii][q] = (q < nb && i < r_hi)
+                        ? ((i < j0 + q) ? T(0) : (i == j0 + q ? T(1) : at(q, i)))
+                        : T(0);
       }
       __syncthreads();
       if (pq >= 0) {
@@ -315,25 +329,33 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
     for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
       t_out[e] = Tm[e / kQrNB][e % kQrNB];
   }
+  if (SM) {
+    for (int q = 0; q < nb; ++q)
+      for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) h[(int64_t)(j0 + q) * mm + i] = at(q, i);
+  }
   cluster.sync();  // CTA 0 has finished reading the others' shared memory
 }
 
-template <typename T>
-static bool qr_cluster_fits(int c) {
+template <typename T, bool SM>
+static bool qr_cluster_fits(int c, size_t smem) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, bool> known;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
   std::lock_guard<std::mutex> lock(mu);
-  const auto key = std::make_pair(dev, c);
+  const auto key = std::make_pair(dev, c * 1000000 + (int)(smem >> 8));
   auto it = known.find(key);
   if (it != known.end()) return it->second;
-  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel<T>,
+  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel<T, SM>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  if (ok && smem > 0)
+    ok = ensure_dynamic_smem(reinterpret_cast<const void*>(qr_panel_cluster_kernel<T, SM>),
+                             (int)smem) == cudaSuccess;
   if (ok) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)c);
     cfg.blockDim = dim3(kQrCluThreads);
+    cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)c;
@@ -342,7 +364,7 @@ static bool qr_cluster_fits(int c) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel<T>, &cfg) ==
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel<T, SM>, &cfg) ==
              cudaSuccess &&
          nclusters >= 1;
   }
@@ -351,18 +373,14 @@ static bool qr_cluster_fits(int c) {
   return ok;
 }
 
-// 0 when the cluster kernel was launched, -1 when the caller must fall back.
-template <typename T>
-static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* t_out,
-                                   cudaStream_t st) {
-  const int64_t rows = mm - j0;
-  int c = (int)((rows + 1023) / 1024);
-  c = c < 1 ? 1 : (c > kQrCluMax ? kQrCluMax : c);
-  if (!qr_cluster_fits<T>(c)) return -1;
-  const int64_t r = (rows + c - 1) / c;
+template <typename T, bool SM>
+static int launch_qr_panel_variant(int c, int64_t r, size_t smem, int64_t mm, int j0, int pe,
+                                   T* h, T* tau, T* t_out, cudaStream_t st) {
+  if (!qr_cluster_fits<T, SM>(c, smem)) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c);
   cfg.blockDim = dim3(kQrCluThreads);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -371,12 +389,28 @@ static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* 
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel<T>, mm, j0, pe, r, h, tau, t_out) !=
+  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel<T, SM>, mm, j0, pe, r, h, tau, t_out) !=
       cudaSuccess) {
     cudaGetLastError();
     return -1;
   }
   return 0;
+}
+
+// 0 when the cluster kernel was launched, -1 when the caller must fall back.
+// The panel's rows stay in shared memory when a CTA's slice fits (FP32).
+template <typename T>
+static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* t_out,
+                                   cudaStream_t st) {
+  const int64_t rows = mm - j0;
+  int c = (int)((rows + 1023) / 1024);
+  c = c < 1 ? 1 : (c > kQrCluMax ? kQrCluMax : c);
+  const int64_t r = (rows + c - 1) / c;
+  const size_t slice = (size_t)kQrNB * r * sizeof(T);
+  if (slice <= 160 * 1024 &&
+      launch_qr_panel_variant<T, true>(c, r, slice, mm, j0, pe, h, tau, t_out, st) == 0)
+    return 0;
+  return launch_qr_panel_variant<T, false>(c, r, 0, mm, j0, pe, h, tau, t_out, st);
 }
 
 // T (nb×nb, upper) of panel rows [j0, j0+nb): T[k][k] = tau_k and
