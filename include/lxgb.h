@@ -117,6 +117,9 @@ int lxgb_potrs_ragged_f64(int64_t batch, int32_t max_n, const int32_t* n,
  * backward error over its right-hand sides.
  * `work` must hold lxgb_posv_ragged_mixed_workspace_size(batch, max_n,
  * max_nrhs) bytes, 256-byte aligned; its contents need no initialisation.
+ * One persistent launch solves the batch; its CTAs take systems largest n
+ * first (a counting sort by n runs ahead of it), so the launch does not end
+ * on a tail of large systems started last.
  * This is the batched form of lineax's Cholesky solve
  * (lineax/_solver/cholesky.py:43-78) with FP64 accuracy recovered by
  * refinement; it has no single-call counterpart in lineax. */
@@ -138,9 +141,11 @@ int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
  * and results are those of lxgb_posv_ragged_mixed without `work`: the scratch
  * is a fixed array of LXGB_POSV_NOALLOC_SCRATCH_BYTES (16 MiB + 256 B) inside
  * the library, which every GPU that loads the library holds until the process
- * exits.  Limits: max_n <= 2048 (larger is rejected with LXGB_INVALID_ARG);
- * systems with n > 224 factor in 16 MiB / (4·max_n²) slices, so fewer CTAs run
- * them than in the workspace form (at max_n = 512, 16 at a time).
+ * exits.  Limits: max_n <= 1024 (larger is rejected with LXGB_INVALID_ARG);
+ * systems with n > 144 factor in 16 MiB / (4·max_n²) slices, so fewer CTAs run
+ * them than in the workspace form (at max_n = 512, 16 at a time); systems are
+ * taken longest first when the slices leave room for the order (4 bytes per
+ * system), else in index order.
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * Every call uses the same array and leaves its contents behind (the call

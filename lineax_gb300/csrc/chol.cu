@@ -2,8 +2,8 @@
 // solve, and the mixed-precision solve (FP32 factor + FP64 refinement).
 //
 // One persistent launch covers a ragged batch: in the mixed path CTAs pull
-// systems from an atomic work queue in index order, in the plain FP64 path
-// they take them round-robin.  Each system is factored by one CTA with
+// systems from an atomic work queue, largest order first (a counting sort by
+// n ahead of the launch), in the plain FP64 path they take them round-robin.  Each system is factored by one CTA with
 // a right-looking blocked algorithm; the matrix is staged in shared memory
 // when it fits and otherwise factored where it lies (FP64 path: in place in
 // the caller's buffer; FP32 path: in a per-CTA slice of the workspace), where
@@ -181,10 +181,11 @@ potrs_ragged_f64_kernel(int64_t batch, int max_n, const int32_t* __restrict__ nv
 //  * factor in FP32 — n <= kMxSmallN: right-looking in shared memory with
 //    16-column panels (diagonal block by one warp, column-parallel TRSM of the
 //    block row, register-tiled SYRK of the trailing matrix: three barriers per
-//    panel); larger n: left-looking by 32-row block rows of U kept in this
+//    panel); larger n: right-looking by 32-row block rows of U kept in this
 //    CTA's workspace slice (an FP32 n×n array, L2-resident while the CTA works
-//    on it), each block row formed by a register-tiled GEMM that streams the
-//    finished rows of U, then its diagonal block and TRSM;
+//    on it) — TRSM of the block row, then a register-tiled SYRK of the
+//    trailing matrix, during which one warp updates and factors the next
+//    diagonal block (lookahead);
 //  * all right-hand sides of a chunk (<= 8) solved together with the FP32
 //    factor (blocked forward/backward substitution, one warp per vector on the
 //    32×32 diagonal blocks, all threads on the off-diagonal updates);
@@ -380,15 +381,19 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
   for (int i = warp; i < n; i += blockDim.x >> 5)
     for (int j = i + lane; j < n; j += 32) U[(int64_t)i * ldu + j] = to_f32(A[(int64_t)i * n + j]);
   __syncthreads();
+  // Lookahead: warp 0 factors the first diagonal block here and every later
+  // one inside the previous block's trailing update (it updates the next
+  // diagonal block's tiles first, then factors them while warps 1.. update the
+  // rest), so the single-warp factorisation no longer idles the CTA.
+  if (warp == 0) {
+    const int bad = warp_potrf_block<kMxNB>(U, ldu, 0, min(kMxNB, n), sm.rd, &sm.ublk[0][0],
+                                            &sm.linv[0][0]);
+    if (lane == 0) sm.flag = bad;
+  }
+  __syncthreads();
+  if (sm.flag) return sm.flag;
   for (int j0 = 0; j0 < n; j0 += kMxNB) {
     const int nb = min(kMxNB, n - j0);
-    if (warp == 0) {
-      const int bad = warp_potrf_block<kMxNB>(U, ldu, j0, nb, sm.rd + j0, &sm.ublk[0][0],
-                                              &sm.linv[0][0]);
-      if (lane == 0) sm.flag = bad;
-    }
-    __syncthreads();
-    if (sm.flag) return sm.flag;
     const int t0 = j0 + nb;          // first trailing row/column
     const int m = n - t0;            // trailing order
     if (m <= 0) break;
@@ -405,15 +410,13 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
       }
       __syncthreads();
     }
-    // 8×8 tiles of the upper triangle of the trailing matrix
+    // 8×8 tiles of the upper triangle of the trailing matrix; the tiles of
+    // the next diagonal block (ti <= tj < dt) belong to warp 0.
     const int mt = (m + 7) >> 3;
     const int ntiles = mt * (mt + 1) / 2;
-    for (int t = tid; t < ntiles; t += blockDim.x) {
-      // (ti, tj) with tj >= ti from the linear index over the triangle
-      int ti = (int)((2.0f * mt + 1.0f - sqrtf((2.0f * mt + 1.0f) * (2.0f * mt + 1.0f) - 8.0f * t)) * 0.5f);
-      while (ti > 0 && ti * (2 * mt - ti + 1) / 2 > t) --ti;
-      while ((ti + 1) * (2 * mt - ti) / 2 <= t) ++ti;
-      const int tj = ti + (t - ti * (2 * mt - ti + 1) / 2);
+    const int nbn = min(kMxNB, m);
+    const int dt = (nbn + 7) >> 3;
+    auto tile = [&](int ti, int tj) {
       const int ri = ti << 3, cj = tj << 3;   // offsets inside the trailing matrix
       float acc[8][8];
 #pragma unroll
@@ -451,8 +454,29 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
         *reinterpret_cast<float4*>(dst) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
         *reinterpret_cast<float4*>(dst + 4) = make_float4(acc[r][4], acc[r][5], acc[r][6], acc[r][7]);
       }
+    };
+    if (warp == 0) {
+      // lane -> (ti, tj) over the dt×dt upper triangle (at most 10 tiles)
+      int t = lane, ti = 0;
+      while (ti < dt && t >= dt - ti) { t -= dt - ti; ++ti; }
+      if (ti < dt) tile(ti, ti + t);
+      __syncwarp();
+      const int bad = warp_potrf_block<kMxNB>(U, ldu, t0, nbn, sm.rd + t0, &sm.ublk[0][0],
+                                              &sm.linv[0][0]);
+      if (lane == 0) sm.flag = bad;
+    } else {
+      for (int t = tid - 32; t < ntiles; t += blockDim.x - 32) {
+        // (ti, tj) with tj >= ti from the linear index over the triangle
+        int ti = (int)((2.0f * mt + 1.0f - sqrtf((2.0f * mt + 1.0f) * (2.0f * mt + 1.0f) - 8.0f * t)) * 0.5f);
+        while (ti > 0 && ti * (2 * mt - ti + 1) / 2 > t) --ti;
+        while ((ti + 1) * (2 * mt - ti) / 2 <= t) ++ti;
+        const int tj = ti + (t - ti * (2 * mt - ti + 1) / 2);
+        if (tj < dt) continue;  // the next diagonal block: warp 0's
+        tile(ti, tj);
+      }
     }
     __syncthreads();
+    if (sm.flag) return sm.flag;
   }
   return 0;
 }
@@ -571,10 +595,12 @@ __device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], flo
 // summation errors go to a second FP32 accumulator.  b - Ax is formed in the
 // same double-float arithmetic from the split of b.  Lane c of each warp
 // finishes vector c.  Per-warp maxima of |r| and the row sums of |A| (for
-// ||A||_inf) land in sm.red / sm.red2.
+// ||A||_inf) land in sm.red / sm.red2.  Vectors nc..NC-1 are padding: b = 0
+// and x = 0 there, so their residual is 0.
 template <int NC>
-__device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, const double* __restrict__ B,
-                              const float* XH, const float* XL, float* D, MxSmem& sm) {
+__device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, int nc,
+                              const double* __restrict__ B, const float* XH, const float* XL,
+                              float* D, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   float rmax = 0.0f;   // lane c: max |r| of vector c
   float rowmax = 0.0f;
@@ -583,7 +609,7 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
 #pragma unroll
     for (int c = 0; c < NC; ++c) { S[c] = 0.0f; C[c] = 0.0f; }
     float rs = 0.0f;
-    const double bval = (lane < NC) ? B[(int64_t)lane * n + i] : 0.0;
+    const double bval = (lane < nc) ? B[(int64_t)lane * n + i] : 0.0;
     const double* row = A + (int64_t)i * n;
     for (int j0 = 0; j0 < n; j0 += 256) {
       double av[8];
@@ -673,15 +699,22 @@ __device__ __noinline__ void mx_update_x(int n, const float* D, float* XH, float
   }
 }
 
-// One refinement chunk of NC vectors: solves, x updates and residuals until
-// every vector's backward error is <= tol or max_iter solves were applied.
+// One refinement chunk of nc <= NC vectors: solves, x updates and residuals
+// until every vector's backward error is <= tol or max_iter solves were
+// applied.  Vectors nc..NC-1 are zero padding, marked done from the start;
+// a vector's arithmetic does not depend on NC or on the other vectors, so its
+// result is the same whichever chunk width solves it.  The kernel instantiates
+// one width (kMxKc) for every count: one copy per count overflowed the
+// instruction cache when the CTAs of an SM ran systems with different
+// right-hand-side counts (ragged 4096-system batch: 11.0 ms with eight
+// widths, 8.6 ms with two, 7.7 ms with one).
 template <int NC>
-__device__ void mx_refine(const float* F, int ld, int n, const double* __restrict__ A,
+__device__ void mx_refine(const float* F, int ld, int n, int nc, const double* __restrict__ A,
                           const double* __restrict__ B, double* __restrict__ X, float* D,
                           float* XH, float* XL, double tol, int max_iter, bool& first_residual,
                           int& iters_out, bool& converged, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  if (tid < kMxKc) { sm.done[tid] = 0; sm.berr[tid] = 0.0; }
+  if (tid < kMxKc) { sm.done[tid] = tid >= nc; sm.berr[tid] = 0.0; }
   // d = fl32(b), x = 0, ||b||_inf
   float bm[NC];
 #pragma unroll
@@ -689,7 +722,7 @@ __device__ void mx_refine(const float* F, int ld, int n, const double* __restric
   for (int i = tid; i < n; i += blockDim.x) {
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      const float v = to_f32(B[(int64_t)c * n + i]);
+      const float v = (c < nc) ? to_f32(B[(int64_t)c * n + i]) : 0.0f;
       D[c * n + i] = v;
       XH[c * n + i] = 0.0f;
       XL[c * n + i] = 0.0f;
@@ -717,7 +750,7 @@ __device__ void mx_refine(const float* F, int ld, int n, const double* __restric
     mx_update_x<NC>(n, D, XH, XL, sm);
     ++it;
     __syncthreads();
-    mx_residual_t<NC>(A, n, B, XH, XL, D, sm);
+    mx_residual_t<NC>(A, n, nc, B, XH, XL, D, sm);
     __syncthreads();
     if (tid == 0) {
       if (first_residual) {
@@ -751,7 +784,7 @@ __device__ void mx_refine(const float* F, int ld, int n, const double* __restric
   for (int i = tid; i < n; i += blockDim.x) {
 #pragma unroll
     for (int c = 0; c < NC; ++c)
-      X[(int64_t)c * n + i] = (double)XH[c * n + i] + (double)XL[c * n + i];
+      if (c < nc) X[(int64_t)c * n + i] = (double)XH[c * n + i] + (double)XL[c * n + i];
   }
   iters_out = it;
   converged = all_done;
@@ -765,19 +798,62 @@ __device__ __forceinline__ int mx_next(int* queue, int* s_next) {
   return *s_next;
 }
 
+// Longest-first order for the work queue: a counting sort of the systems by
+// n, descending (one CTA; ties in no particular order — a system's result does
+// not depend on which CTA solves it).  Systems with n outside [0, kMxMaxN]
+// are rejected by the solve and go last.  Also clears the queue counter.
+constexpr int kOrderThreads = 1024;
+constexpr int kOrderBins = kMxMaxN + 2;
+
+__global__ void __launch_bounds__(kOrderThreads)
+order_systems_kernel(int64_t batch, const int32_t* __restrict__ nvec, int32_t* __restrict__ order,
+                     int* queue) {
+  __shared__ int bins[kOrderBins];
+  __shared__ int chunk_sum[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto bin_of = [](int n) { return (n < 0 || n > kMxMaxN) ? kOrderBins - 1 : kMxMaxN - n; };
+  for (int i = tid; i < kOrderBins; i += kOrderThreads) bins[i] = 0;
+  __syncthreads();
+  for (int64_t s = tid; s < batch; s += kOrderThreads) atomicAdd(&bins[bin_of(nvec[s])], 1);
+  __syncthreads();
+  // exclusive scan of the bins: warp 0, each lane a contiguous chunk
+  constexpr int kChunk = (kOrderBins + 31) / 32;
+  if (warp == 0) {
+    const int lo = lane * kChunk, hi = min(lo + kChunk, kOrderBins);
+    int sum = 0;
+    for (int i = lo; i < hi; ++i) sum += bins[i];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    chunk_sum[lane] = incl - sum;
+    __syncwarp();
+    int run = chunk_sum[lane];
+    for (int i = lo; i < hi; ++i) { const int c = bins[i]; bins[i] = run; run += c; }
+  }
+  __syncthreads();
+  for (int64_t s = tid; s < batch; s += kOrderThreads)
+    order[atomicAdd(&bins[bin_of(nvec[s])], 1)] = (int32_t)s;
+  if (tid == 0) *queue = 0;
+}
+
 __global__ void __launch_bounds__(kMxThreads, 2)
 posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restrict__ nvec,
                   const int32_t* __restrict__ nrhs_vec, const int64_t* __restrict__ a_off,
                   const double* __restrict__ a, const int64_t* __restrict__ b_off,
                   const double* __restrict__ b, double* __restrict__ x, double tol, int max_iter,
                   int32_t* __restrict__ info, int32_t* __restrict__ iters,
-                  double* __restrict__ berr_out, int* queue, float* __restrict__ factor_ws) {
+                  double* __restrict__ berr_out, int* queue, const int32_t* __restrict__ order,
+                  float* __restrict__ factor_ws) {
   extern __shared__ float smem_mx[];
   __shared__ MxSmem sm;
   const int tid = threadIdx.x;
   for (;;) {
-    const int s = mx_next(queue, &sm.next);
-    if (s >= batch) break;
+    const int k = mx_next(queue, &sm.next);
+    if (k >= batch) break;
+    const int s = order ? order[k] : k;
     const int n = nvec[s];
     const int nrhs = nrhs_vec[s];
     if (n > max_n || n < 0 || nrhs > max_nrhs || nrhs < 0) {
@@ -825,16 +901,7 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
       double* X = x + b_off[s] + (int64_t)c0 * n;
       int it = 0;
       bool conv = true;
-      switch (nc) {
-        case 1: mx_refine<1>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 2: mx_refine<2>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 3: mx_refine<3>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 4: mx_refine<4>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 5: mx_refine<5>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 6: mx_refine<6>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        case 7: mx_refine<7>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-        default: mx_refine<8>(F, ld, n, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm); break;
-      }
+      mx_refine<kMxKc>(F, ld, n, nc, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm);
       if (!conv) sys_info = -1;
       for (int c = 0; c < nc; ++c) sys_berr = fmax(sys_berr, sm.berr[c]);
       sys_iters = max(sys_iters, it);
@@ -856,8 +923,11 @@ static size_t mixed_smem_bytes(int max_n, int max_nrhs) {
   return small > large ? small : large;
 }
 
-// Workspace: queue header + one FP32 max_n² factor slice per CTA when some
-// system can exceed the shared-memory size.
+// Workspace: queue header, the longest-first order (batch int32, rounded up
+// to 256 bytes), then one FP32 max_n² factor slice per CTA when some system
+// can exceed the shared-memory size.
+static int64_t mixed_order_bytes(int64_t batch) { return (batch * 4 + 255) & ~(int64_t)255; }
+
 static int64_t mixed_slice_bytes(int max_n) {
   const int64_t ld = (max_n + 31) & ~31;
   return (max_n > kMxSmallN) ? ld * ld * (int64_t)sizeof(float) : 0;
@@ -868,21 +938,28 @@ static int mixed_grid(int64_t batch) {
   return (int)((batch < g) ? batch : g);
 }
 
-// Launch over `grid` CTAs with the given scratch (queue + factor slices).
+// Launch over `grid` CTAs with the given scratch (queue [+ order] + factor
+// slices).  Without the order (ordered == false) systems go in index order.
 static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs, const int32_t* n,
                         const int32_t* nrhs, const int64_t* a_off, const double* a,
                         const int64_t* b_off, const double* b, double* x, double tol,
                         int32_t max_iter, int32_t* info, int32_t* iters, double* berr,
-                        void* scratch, cudaStream_t st) {
-  int* queue = reinterpret_cast<int*>(scratch);
-  float* factor_ws = reinterpret_cast<float*>(reinterpret_cast<char*>(scratch) + kQueueHeader);
-  reset_queue_kernel<<<1, 1, 0, st>>>(queue);
+                        void* scratch, bool ordered, cudaStream_t st) {
+  char* base = reinterpret_cast<char*>(scratch);
+  int* queue = reinterpret_cast<int*>(base);
+  int32_t* order = ordered ? reinterpret_cast<int32_t*>(base + kQueueHeader) : nullptr;
+  float* factor_ws = reinterpret_cast<float*>(
+      base + kQueueHeader + (ordered ? mixed_order_bytes(batch) : 0));
+  if (ordered)
+    order_systems_kernel<<<1, kOrderThreads, 0, st>>>(batch, n, order, queue);
+  else
+    reset_queue_kernel<<<1, 1, 0, st>>>(queue);
   const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
   LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(posv_mixed_kernel), (int)smem),
                 "posv_mixed: set smem");
   posv_mixed_kernel<<<(unsigned)grid, kMxThreads, smem, st>>>(
       batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
-      queue, factor_ws);
+      queue, order, factor_ws);
   return check_launch("posv_mixed");
 }
 
@@ -928,7 +1005,8 @@ extern "C" int64_t lxgb_posv_ragged_mixed_workspace_size(int64_t batch, int32_t 
                                                          int32_t max_nrhs) {
   (void)max_nrhs;
   if (batch <= 0 || max_n <= 0) return kQueueHeader;
-  return kQueueHeader + (int64_t)mixed_grid(batch) * mixed_slice_bytes(max_n);
+  return kQueueHeader + mixed_order_bytes(batch) +
+         (int64_t)mixed_grid(batch) * mixed_slice_bytes(max_n);
 }
 
 extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
@@ -950,7 +1028,7 @@ extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_
     return LXGB_WORKSPACE_TOO_SMALL;
   }
   return mixed_launch(mixed_grid(batch), batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x,
-                      tol, max_iter, info, iters, berr, work, as_stream(stream));
+                      tol, max_iter, info, iters, berr, work, true, as_stream(stream));
 }
 
 // ---------------------------------------------------------------------------
@@ -1012,11 +1090,14 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
   LXGB_REQUIRE(max_n <= kMxMaxN,
                "posv_mixed_noalloc: max_n above 1024");
   // Grid: one FP32 factor slice per CTA for systems above the shared-memory
-  // size, as many slices as the fixed scratch holds.
+  // size, as many slices as the fixed scratch holds.  The longest-first order
+  // goes in what the slices leave over; without room for it systems go in
+  // index order.
   int64_t grid = mixed_grid(batch);
   const int64_t slice = mixed_slice_bytes(max_n);
+  const int64_t room = (int64_t)LXGB_POSV_NOALLOC_SCRATCH_BYTES - kQueueHeader;
   if (slice > 0) {
-    const int64_t slices = (int64_t)(LXGB_POSV_NOALLOC_SCRATCH_BYTES - kQueueHeader) / slice;
+    const int64_t slices = room / slice;
     if (slices < 1) {
       set_last_error("posv_mixed_noalloc: max_n=%d needs %lld bytes of scratch, limit %lld", max_n,
                      (long long)(slice + kQueueHeader),
@@ -1025,11 +1106,12 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
     }
     if (slices < grid) grid = slices;
   }
+  const bool ordered = mixed_order_bytes(batch) + grid * slice <= room;
   void* scratch = nullptr;
   int rc = noalloc_scratch_address(&scratch);
   if (rc) return rc;
   // mixed_launch clears the work-queue counter, which the array keeps from the
   // previous call.
   return mixed_launch((int)grid, batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol,
-                      max_iter, info, iters, berr, scratch, as_stream(stream));
+                      max_iter, info, iters, berr, scratch, ordered, as_stream(stream));
 }
