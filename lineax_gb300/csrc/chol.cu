@@ -220,6 +220,76 @@ struct MxSmem {
 };
 
 
+// Split W FP64 values with one warp vote (see split_f64).
+template <int W>
+__device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], float (&lo)[W]) {
+  bool slow = false;
+#pragma unroll
+  for (int u = 0; u < W; ++u) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]);
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned mh = (unsigned)(b >> 29) & 0x7FFFFFu;
+    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;
+    const int sh = __clz(rem | 1u) - 8;
+    const unsigned m = (sh >= 0) ? (rem << sh) : (rem >> (-sh));
+    const int ex = (int)e - 1052 - sh + 127;
+    const bool zero = (b << 1) == 0ull;
+    hi[u] = zero ? __uint_as_float(sign) : __uint_as_float(sign | (((e - 1023u + 127u) & 0xFFu) << 23) | mh);
+    lo[u] = (rem == 0u) ? 0.0f : __uint_as_float(sign | (((unsigned)ex & 0xFFu) << 23) | (m & 0x7FFFFFu));
+    slow |= !zero && ((e < 949u) || (e > 1150u));
+  }
+  if (__any_sync(__activemask(), slow)) {
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a[u]) >> 52) & 0x7FFu;
+      if (a[u] != 0.0 && ((e < 949u) || (e > 1150u))) {
+        hi[u] = __double2float_rz(a[u]);
+        lo[u] = __double2float_rn(a[u] - (double)hi[u]);
+      }
+    }
+  }
+}
+
+// FP32 copy (the hi part of split_f64) of the upper triangle of the row-major
+// n×n FP64 matrix A into F (row stride ld).  A warp walks 256-column chunks of
+// its rows (j >= i); the next chunk's eight loads per lane are issued before
+// the current one is converted, so two chunks are in flight (the copy streams
+// A from DRAM and was latency-bound one chunk at a time).
+__device__ __forceinline__ void mx_copy_upper(const double* __restrict__ A, int n, float* F,
+                                              int64_t ld) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  auto load = [&](int r, int j0, double (&v)[8]) {
+    const double* arow = A + (int64_t)r * n;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = j0 + lane + 32 * u;
+      v[u] = (r < n && j < n) ? arow[j] : 0.0;
+    }
+  };
+  int i = warp, j0 = warp;
+  double v[8];
+  load(i, j0, v);
+  while (i < n) {
+    int ni = i, nj = j0 + 256;
+    if (nj >= n) { ni = i + nw; nj = ni; }
+    double vn[8];
+    load(ni, nj, vn);
+    float hi[8], lo[8];
+    splitw<8>(v, hi, lo);
+    float* frow = F + (int64_t)i * ld;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = j0 + lane + 32 * u;
+      if (j < n) frow[j] = hi[u];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = vn[u];
+    i = ni;
+    j0 = nj;
+  }
+}
+
 // Factor the nb×nb diagonal block at F[j0.., j0..] (upper triangle, row
 // stride ld) by one warp entirely in registers: lane j holds column j; row k
 // of U is formed in place and rows i > k updated with u_ki fetched by shuffle.
@@ -377,9 +447,7 @@ struct MxStage {
 __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
                                MxStage& st) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // FP32 copy of the upper triangle
-  for (int i = warp; i < n; i += blockDim.x >> 5)
-    for (int j = i + lane; j < n; j += 32) U[(int64_t)i * ldu + j] = to_f32(A[(int64_t)i * n + j]);
+  mx_copy_upper(A, n, U, ldu);
   __syncthreads();
   // Lookahead: warp 0 factors the first diagonal block here and every later
   // one inside the previous block's trailing update (it updates the next
@@ -487,9 +555,47 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
 // (forward) or row (backward) of the block into registers first, so the
 // sequential steps only exchange values by shuffles; the off-diagonal
 // updates take one matrix row or column per thread for all NC vectors.
+// Off-diagonal updates of the blocked substitution for the first W vectors
+// of D (the rest are padding): rows below block [r0, r0+rn) in the forward
+// pass, rows above it in the backward pass; one matrix row per thread.
+template <int W>
+__device__ __forceinline__ void mx_solve_rows_below(const float* U, int ld, int n, int r0, int rn,
+                                                    float* D) {
+  for (int i = r0 + rn + threadIdx.x; i < n; i += blockDim.x) {
+    float v[W];
+#pragma unroll
+    for (int c = 0; c < W; ++c) v[c] = D[c * n + i];
+    for (int t = 0; t < rn; ++t) {
+      const float u = U[(r0 + t) * ld + i];
+#pragma unroll
+      for (int c = 0; c < W; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < W; ++c) D[c * n + i] = v[c];
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void mx_solve_rows_above(const float* U, int ld, int n, int r0, int rn,
+                                                    float* D) {
+  for (int i = threadIdx.x; i < r0; i += blockDim.x) {
+    const float* rowp = U + i * ld + r0;
+    float v[W];
+#pragma unroll
+    for (int c = 0; c < W; ++c) v[c] = D[c * n + i];
+    for (int t = 0; t < rn; ++t) {
+      const float u = rowp[t];
+#pragma unroll
+      for (int c = 0; c < W; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < W; ++c) D[c * n + i] = v[c];
+  }
+}
+
 template <int NC>
-__device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, float* D, const float* rd,
-                           const MxSmem& sm) {
+__device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, float* D,
+                                        const float* rd, const MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nw = blockDim.x >> 5;
   const int nblk = (n + 31) >> 5;
@@ -510,18 +616,10 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, float* D,
       if (lane < rn) D[c * n + r0 + lane] = v;
     }
     __syncthreads();
-    for (int i = r0 + rn + tid; i < n; i += blockDim.x) {
-      float v[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) v[c] = D[c * n + i];
-      for (int t = 0; t < rn; ++t) {
-        const float u = U[(r0 + t) * ld + i];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
-      }
-#pragma unroll
-      for (int c = 0; c < NC; ++c) D[c * n + i] = v[c];
-    }
+    if (nc <= NC / 2)
+      mx_solve_rows_below<NC / 2>(U, ld, n, r0, rn, D);
+    else
+      mx_solve_rows_below<NC>(U, ld, n, r0, rn, D);
     __syncthreads();
   }
   for (int bi = nblk - 1; bi >= 0; --bi) {  // backward: U x = y
@@ -541,51 +639,11 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, float* D,
       if (lane < rn) D[c * n + r0 + lane] = v;
     }
     __syncthreads();
-    for (int i = tid; i < r0; i += blockDim.x) {
-      const float* rowp = U + i * ld + r0;
-      float v[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) v[c] = D[c * n + i];
-      for (int t = 0; t < rn; ++t) {
-        const float u = rowp[t];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
-      }
-#pragma unroll
-      for (int c = 0; c < NC; ++c) D[c * n + i] = v[c];
-    }
+    if (nc <= NC / 2)
+      mx_solve_rows_above<NC / 2>(U, ld, n, r0, rn, D);
+    else
+      mx_solve_rows_above<NC>(U, ld, n, r0, rn, D);
     __syncthreads();
-  }
-}
-
-// Split W FP64 values with one warp vote (see split_f64).
-template <int W>
-__device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], float (&lo)[W]) {
-  bool slow = false;
-#pragma unroll
-  for (int u = 0; u < W; ++u) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]);
-    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-    const unsigned mh = (unsigned)(b >> 29) & 0x7FFFFFu;
-    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;
-    const int sh = __clz(rem | 1u) - 8;
-    const unsigned m = (sh >= 0) ? (rem << sh) : (rem >> (-sh));
-    const int ex = (int)e - 1052 - sh + 127;
-    const bool zero = (b << 1) == 0ull;
-    hi[u] = zero ? __uint_as_float(sign) : __uint_as_float(sign | (((e - 1023u + 127u) & 0xFFu) << 23) | mh);
-    lo[u] = (rem == 0u) ? 0.0f : __uint_as_float(sign | (((unsigned)ex & 0xFFu) << 23) | (m & 0x7FFFFFu));
-    slow |= !zero && ((e < 949u) || (e > 1150u));
-  }
-  if (__any_sync(__activemask(), slow)) {
-#pragma unroll
-    for (int u = 0; u < W; ++u) {
-      const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a[u]) >> 52) & 0x7FFu;
-      if (a[u] != 0.0 && ((e < 949u) || (e > 1150u))) {
-        hi[u] = __double2float_rz(a[u]);
-        lo[u] = __double2float_rn(a[u] - (double)hi[u]);
-      }
-    }
   }
 }
 
@@ -601,70 +659,129 @@ template <int NC>
 __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, int nc,
                               const double* __restrict__ B, const float* XH, const float* XL,
                               float* D, MxSmem& sm) {
+  static_assert(NC == 8, "the transposing reduction below is written for 8 vectors");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  float rmax = 0.0f;   // lane c: max |r| of vector c
+  const int cl = lane >> 2;            // the vector this lane finishes (lanes 4c..4c+3)
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  float rmax = 0.0f;                   // lane 4c: max |r| of vector c
   float rowmax = 0.0f;
+  // The warp walks (row, 256-column chunk) pairs; the loads of the next pair
+  // (and b of the next row) are issued before the current chunk is used, so
+  // the DRAM latency of A overlaps the arithmetic.
+  const int nch = (n + 255) >> 8;
+  auto load_chunk = [&](int r, int ch, double (&v)[8]) {
+    const double* rowp = A + (int64_t)r * n;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = (ch << 8) + lane + 32 * u;
+      v[u] = (r < n && j < n) ? rowp[j] : 0.0;
+    }
+  };
+  double av[8];
+  load_chunk(warp, 0, av);
+  double bnext = (warp < n && cl < nc) ? B[(int64_t)cl * n + warp] : 0.0;
   for (int i = warp; i < n; i += nw) {
     float S[NC], C[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) { S[c] = 0.0f; C[c] = 0.0f; }
     float rs = 0.0f;
-    const double bval = (lane < nc) ? B[(int64_t)lane * n + i] : 0.0;
-    const double* row = A + (int64_t)i * n;
-    for (int j0 = 0; j0 < n; j0 += 256) {
-      double av[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int j = j0 + lane + 32 * u;
-        av[u] = (j < n) ? row[j] : 0.0;
+    const double bval = bnext;
+    for (int ch = 0; ch < nch; ++ch) {
+      const int j0 = ch << 8;
+      double an[8];
+      if (ch + 1 < nch) {
+        load_chunk(i, ch + 1, an);
+      } else {
+        load_chunk(i + nw, 0, an);
+        bnext = (i + nw < n && cl < nc) ? B[(int64_t)cl * n + i + nw] : 0.0;
       }
       float ah[8], al[8];
       splitw<8>(av, ah, al);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int j = j0 + lane + 32 * u;
-        if (j < n) {
-          rs += fabsf(ah[u]);
+      for (int u = 0; u < 8; ++u) rs += fabsf(ah[u]);   // ah = 0 past the row's end
+      // vectors 0..3, then 4..7 only when the chunk has more than four live
+      // ones (the rest are padding); per vector the terms go in j order
 #pragma unroll
-          for (int c = 0; c < NC; ++c) {
-            const float xh = XH[c * n + j], xl = XL[c * n + j];
-            const float p = ah[u] * xh;
-            const float pe = fmaf(ah[u], xh, -p);
-            float err;
-            two_sum(S[c], p, err);
-            C[c] += fmaf(ah[u], xl, fmaf(al[u], xh, pe + err));
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && nc <= 4) break;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int j = j0 + lane + 32 * u;
+          if (j < n) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int c = 4 * h + k;
+              const float xh = XH[c * n + j], xl = XL[c * n + j];
+              const float p = ah[u] * xh;
+              const float pe = fmaf(ah[u], xh, -p);
+              float err;
+              two_sum(S[c], p, err);
+              C[c] += fmaf(ah[u], xl, fmaf(al[u], xh, pe + err));
+            }
           }
         }
       }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) av[u] = an[u];
+    }
+    // Transposing butterfly: each exchange halves the vectors a lane keeps
+    // (xor 16: 4 of 8, xor 8: 2, xor 4: 1), then two plain steps; lane L ends
+    // with the row's sum for vector L >> 2.  Nine double-float additions per
+    // lane instead of forty.
+    float S4[4], C4[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float ss = __shfl_xor_sync(0xffffffffu, b4 ? S[k] : S[4 + k], 16);
+      const float cs = __shfl_xor_sync(0xffffffffu, b4 ? C[k] : C[4 + k], 16);
+      S4[k] = b4 ? S[4 + k] : S[k];
+      C4[k] = b4 ? C[4 + k] : C[k];
+      float err;
+      two_sum(S4[k], ss, err);
+      C4[k] += cs + err;
+    }
+    float S2[2], C2[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float ss = __shfl_xor_sync(0xffffffffu, b3 ? S4[k] : S4[2 + k], 8);
+      const float cs = __shfl_xor_sync(0xffffffffu, b3 ? C4[k] : C4[2 + k], 8);
+      S2[k] = b3 ? S4[2 + k] : S4[k];
+      C2[k] = b3 ? C4[2 + k] : C4[k];
+      float err;
+      two_sum(S2[k], ss, err);
+      C2[k] += cs + err;
+    }
+    float S1, C1;
+    {
+      const float ss = __shfl_xor_sync(0xffffffffu, b2 ? S2[0] : S2[1], 4);
+      const float cs = __shfl_xor_sync(0xffffffffu, b2 ? C2[0] : C2[1], 4);
+      S1 = b2 ? S2[1] : S2[0];
+      C1 = b2 ? C2[1] : C2[0];
+      float err;
+      two_sum(S1, ss, err);
+      C1 += cs + err;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      rs += __shfl_xor_sync(0xffffffffu, rs, o);
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const float s2 = __shfl_xor_sync(0xffffffffu, S[c], o);
-        const float c2 = __shfl_xor_sync(0xffffffffu, C[c], o);
-        float err;
-        two_sum(S[c], s2, err);
-        C[c] += c2 + err;
-      }
+    for (int o = 2; o > 0; o >>= 1) {
+      const float ss = __shfl_xor_sync(0xffffffffu, S1, o);
+      const float cs = __shfl_xor_sync(0xffffffffu, C1, o);
+      float err;
+      two_sum(S1, ss, err);
+      C1 += cs + err;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
     rowmax = fmaxf(rowmax, rs);
-    float Sl = 0.0f, Cl = 0.0f;
-#pragma unroll
-    for (int c = 0; c < NC; ++c)
-      if (lane == c) { Sl = S[c]; Cl = C[c]; }
-    if (lane < NC) {
+    if ((lane & 3) == 0) {
       float bh, bl;
       split_f64(bval, bh, bl);
       float rh = bh, re;
-      two_sum(rh, -Sl, re);
-      const float r = rh + ((bl - Cl) + re);
-      D[lane * n + i] = r;
+      two_sum(rh, -S1, re);
+      const float r = rh + ((bl - C1) + re);
+      D[cl * n + i] = r;
       rmax = fmaxf(rmax, fabsf(r));
     }
   }
-  if (lane < kMxKc) sm.red[warp][lane] = (lane < NC) ? rmax : 0.0f;
+  if ((lane & 3) == 0) sm.red[warp][cl] = rmax;
   if (lane == 0) sm.red2[warp][0] = rowmax;
 }
 
@@ -746,7 +863,7 @@ __device__ void mx_refine(const float* F, int ld, int n, int nc, const double* _
   int it = 0;
   bool all_done = false;
   for (;;) {
-    mx_solve_t<NC>(F, ld, n, D, sm.rd, sm);
+    mx_solve_t<NC>(F, ld, n, nc, D, sm.rd, sm);
     mx_update_x<NC>(n, D, XH, XL, sm);
     ++it;
     __syncthreads();
@@ -876,10 +993,7 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
     if (tid == 0) sm.flag = 0;
     int rc;
     if (small) {
-      for (int e = tid; e < n * n; e += blockDim.x) {
-        const int i = e / n, j = e - i * n;
-        if (j >= i) F[i * ld + j] = to_f32(A[e]);
-      }
+      mx_copy_upper(A, n, F, ld);
       __syncthreads();
       rc = mx_factor_small(F, ld, n, sm);
     } else {
