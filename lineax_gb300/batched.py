@@ -199,39 +199,101 @@ class CapturedMixedSolve:
         return self.out
 
 
-class HostRaggedSPDSolver:
-    """Solve ragged SPD batches whose data lives in host memory.
+class _HostSet:
+    """One set of device buffers of HostRaggedSPDSolver (matrices, right-hand
+    sides, results), cut into chunks."""
 
-    Device buffers, metadata and the workspace are allocated once for a fixed
-    layout (n_list, nrhs_list); each call copies the matrices and right-hand
-    sides in from (pinned) host tensors on the current stream, runs the
-    mixed-precision solve, and copies solutions and per-system status back.
-    """
-
-    def __init__(self, n_list, nrhs_list, tol: float = 1e-12, max_iter: int = 10,
-                 device="cuda"):
+    def __init__(self, n_list, nrhs_list, chunks: int, device):
         a_off, b_off, ta, tb = RaggedBatch.layout(n_list, nrhs_list)
+        nb = len(n_list)
         self.a_dev = torch.empty(ta, dtype=torch.float64, device=device)
         self.b_dev = torch.empty(tb, dtype=torch.float64, device=device)
-        self.batch = RaggedBatch.from_packed(self.a_dev, self.b_dev, n_list, nrhs_list, device)
-        self.ws = MixedWorkspace(self.batch.batch, self.batch.max_n, self.batch.max_nrhs, device)
-        nb = self.batch.batch
         self.out = MixedResult(
             x=torch.empty(tb, dtype=torch.float64, device=device),
             info=torch.empty(nb, dtype=torch.int32, device=device),
             iters=torch.empty(nb, dtype=torch.int32, device=device),
             berr=torch.empty(nb, dtype=torch.float64, device=device),
         )
+        # chunk boundaries: contiguous system ranges of about equal bytes
+        k = max(1, min(int(chunks), nb))
+        sizes = [n * n + n * r for n, r in zip(n_list, nrhs_list)]
+        total = float(sum(sizes)) or 1.0
+        bounds, acc = [0], 0
+        for s_, sz in enumerate(sizes):
+            acc += sz
+            if len(bounds) < k and acc >= total * len(bounds) / k and s_ + 1 < nb:
+                bounds.append(s_ + 1)
+        bounds.append(nb)
+        self.chunks = []
+        for lo, hi in zip(bounds[:-1], bounds[1:]):
+            a0, b0 = a_off[lo], b_off[lo]
+            a1 = a_off[hi] if hi < nb else ta
+            b1 = b_off[hi] if hi < nb else tb
+            sub = RaggedBatch.from_packed(self.a_dev[a0:a1], self.b_dev[b0:b1],
+                                          list(n_list[lo:hi]), list(nrhs_list[lo:hi]), device)
+            res = MixedResult(x=self.out.x[b0:b1], info=self.out.info[lo:hi],
+                              iters=self.out.iters[lo:hi], berr=self.out.berr[lo:hi])
+            self.chunks.append((lo, hi, a0, a1, b0, b1, sub, res))
+        self.copied = [torch.cuda.Event() for _ in self.chunks]
+        self.released = torch.cuda.Event()   # the last solve that read this set
+        self.used = False
+
+
+class HostRaggedSPDSolver:
+    """Solve ragged SPD batches whose data lives in host memory.
+
+    Device buffers, metadata and the workspace are allocated once for a fixed
+    layout (n_list, nrhs_list); each call copies the matrices and right-hand
+    sides in from (pinned) host tensors, runs the mixed-precision solve, and
+    copies solutions and per-system status back into host tensors.  Calls are
+    asynchronous (stream-ordered on the caller's current stream): read the
+    results, or change the host inputs, after synchronising.
+
+    Overlap: host-to-device copies run on a side stream.  With `buffers` >= 2
+    device buffer sets, calls rotate through them, so the copy of call k+1
+    runs while call k is solved (a set is refilled once the solve that last
+    read it has finished).  With `chunks` > 1 the systems of a call are also
+    cut into contiguous ranges of about equal bytes, and the solve of chunk j
+    waits only for chunk j's copy.  A system's result does not depend on
+    either setting.
+    """
+
+    def __init__(self, n_list, nrhs_list, tol: float = 1e-12, max_iter: int = 10,
+                 device="cuda", chunks: int = 1, buffers: int = 2):
+        self.sets = [_HostSet(n_list, nrhs_list, chunks, device) for _ in range(max(1, buffers))]
+        first = self.sets[0]
+        self.out, self.chunks = first.out, first.chunks
+        self.batch = RaggedBatch.from_packed(first.a_dev, first.b_dev, n_list, nrhs_list, device)
         self.tol, self.max_iter = tol, max_iter
-        self.h2d_bytes = (ta + tb) * 8
-        self.d2h_bytes = tb * 8 + nb * (4 + 4 + 8)
+        nb = len(n_list)
+        self.h2d_bytes = (first.a_dev.numel() + first.b_dev.numel()) * 8
+        self.d2h_bytes = first.b_dev.numel() * 8 + nb * (4 + 4 + 8)
+        self.ws = MixedWorkspace(max(c[6].batch for c in first.chunks),
+                                 max(c[6].max_n for c in first.chunks),
+                                 max(c[6].max_nrhs for c in first.chunks), device)
+        self.copy_stream = torch.cuda.Stream(device=device)
+        self.calls = 0
 
     def __call__(self, a_host: torch.Tensor, b_host: torch.Tensor, x_host: torch.Tensor,
                  info_host: torch.Tensor, iters_host: torch.Tensor, berr_host: torch.Tensor):
-        self.a_dev.copy_(a_host, non_blocking=True)
-        self.b_dev.copy_(b_host, non_blocking=True)
-        spd_solve_ragged_mixed(self.batch, self.tol, self.max_iter, self.ws, self.out)
-        x_host.copy_(self.out.x, non_blocking=True)
-        info_host.copy_(self.out.info, non_blocking=True)
-        iters_host.copy_(self.out.iters, non_blocking=True)
-        berr_host.copy_(self.out.berr, non_blocking=True)
+        st = self.sets[self.calls % len(self.sets)]
+        self.calls += 1
+        main = torch.cuda.current_stream(st.a_dev.device)
+        if st.used:
+            self.copy_stream.wait_event(st.released)
+        else:
+            self.copy_stream.wait_stream(main)
+            st.used = True
+        with torch.cuda.stream(self.copy_stream):
+            for (lo, hi, a0, a1, b0, b1, sub, res), ev in zip(st.chunks, st.copied):
+                st.a_dev[a0:a1].copy_(a_host[a0:a1], non_blocking=True)
+                st.b_dev[b0:b1].copy_(b_host[b0:b1], non_blocking=True)
+                ev.record(self.copy_stream)
+        for (lo, hi, a0, a1, b0, b1, sub, res), ev in zip(st.chunks, st.copied):
+            main.wait_event(ev)
+            spd_solve_ragged_mixed(sub, self.tol, self.max_iter, self.ws, res)
+            x_host[b0:b1].copy_(res.x, non_blocking=True)
+            info_host[lo:hi].copy_(res.info, non_blocking=True)
+            iters_host[lo:hi].copy_(res.iters, non_blocking=True)
+            berr_host[lo:hi].copy_(res.berr, non_blocking=True)
+        st.released.record(main)

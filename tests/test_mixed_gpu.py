@@ -124,3 +124,38 @@ def test_mixed_captured_graph_replay_matches_direct_call(dev):
     torch.cuda.synchronize()
     assert torch.equal(out.x, again.x)
     assert float(out.berr.max()) <= 1e-12
+
+
+@pytest.mark.parametrize("chunks,buffers", [(1, 1), (3, 1), (8, 2), (1, 2)])
+def test_host_solver_chunked_copies_match_device_solve(dev, chunks, buffers):
+    """The host-buffer solver (copies overlapping solves: later chunks of a
+    call, or the next call into the other buffer set) returns the same bits
+    as one device-resident solve, and later calls with new data solve the new
+    data."""
+    rng = np.random.default_rng(33)
+    ns = [512, 300, 200, 145, 144, 100, 64, 33, 17, 16, 250, 90]
+    ks = [1 + (3 * i) % 8 for i in range(len(ns))]
+    mats, rhs = make_ragged(rng, ns, ks)
+    rb = to_batch(mats, rhs, dev)
+    ref = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    hs = batched.HostRaggedSPDSolver(ns, ks, TOL, device=dev, chunks=chunks, buffers=buffers)
+    assert len(hs.chunks) == min(chunks, len(ns))
+    a_h = rb.a.cpu().pin_memory()
+    b_h = rb.b.cpu().pin_memory()
+    x_h = torch.empty(rb.b.numel(), dtype=torch.float64).pin_memory()
+    i_h = torch.empty(len(ns), dtype=torch.int32).pin_memory()
+    it_h = torch.empty(len(ns), dtype=torch.int32).pin_memory()
+    be_h = torch.empty(len(ns), dtype=torch.float64).pin_memory()
+    hs(a_h, b_h, x_h, i_h, it_h, be_h)
+    torch.cuda.synchronize()
+    assert torch.equal(x_h, ref.x.cpu())
+    assert torch.equal(i_h, ref.info.cpu()) and torch.equal(it_h, ref.iters.cpu())
+    assert torch.equal(be_h, ref.berr.cpu())
+    for scale in (-3.0, 0.5, 2.0):
+        b_h.mul_(scale)
+        hs(a_h, b_h, x_h, i_h, it_h, be_h)
+        torch.cuda.synchronize()
+        rb.b.mul_(scale)
+        ref2 = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+        torch.cuda.synchronize()
+        assert torch.equal(x_h, ref2.x.cpu())
