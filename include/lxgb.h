@@ -231,6 +231,42 @@ int lxgb_cg_status(int32_t k, int64_t n, int32_t parity, int32_t* steps,
                    int32_t* active, void* work, int64_t work_bytes,
                    void* stream);
 
+/* BiCGStab (lineax/_solver/bicgstab.py:78-205), right-preconditioned, FP64,
+ * for k right-hand sides stored back to back (vector c at base + c*n).  Each
+ * right-hand side has its own scalars and a flag from lineax's loop condition
+ * (no breakdown, stopping test not met, step < max_steps); every call leaves
+ * an inactive right-hand side untouched.  Host sequence: r = b - A y0, then
+ * lxgb_bicgstab_start(r -> r0 copy, p = v = 0); per iteration
+ *   lxgb_bicgstab_direction  (rho' = <r0, r>, p = r + beta (p - omega v)),
+ *   x = M p, v = A x,
+ *   lxgb_bicgstab_s          (alpha = rho'/<r0, v>, s = r - alpha v),
+ *   z = M s, t = A z,
+ *   lxgb_bicgstab_update     (omega = <s,t>/<t,t>, y += alpha x + omega z,
+ *                             r = s - omega t, stopping test, next flag).
+ * lxgb_bicgstab_status copies steps, flags, (rho, alpha, omega) as three
+ * k-arrays and the last "not converged" value to device arrays (any may be
+ * NULL); with them the caller forms lineax's result codes (:188-202).
+ * r must not alias s, t, x or z; y must not alias x, z, s or t. */
+int64_t lxgb_bicgstab_workspace_size(int32_t nrhs, int64_t n);
+int lxgb_bicgstab_start(int32_t k, int64_t n, const double* r, double* r0,
+                        double* p, double* v, int64_t max_steps,
+                        int32_t has_scale, void* work, int64_t work_bytes,
+                        void* stream);
+int lxgb_bicgstab_direction(int32_t k, int64_t n, const double* r0,
+                            const double* r, const double* v, double* p,
+                            void* work, int64_t work_bytes, void* stream);
+int lxgb_bicgstab_s(int32_t k, int64_t n, const double* r0, const double* r,
+                    const double* v, double* s, void* work, int64_t work_bytes,
+                    void* stream);
+int lxgb_bicgstab_update(int32_t k, int64_t n, const double* x, const double* z,
+                         const double* s, const double* t, const double* b,
+                         double* y, double* r, double rtol, double atol,
+                         int64_t max_steps, int32_t has_scale, void* work,
+                         int64_t work_bytes, void* stream);
+int lxgb_bicgstab_status(int32_t k, int64_t n, int32_t* steps, int32_t* active,
+                         double* scal, int32_t* nc, void* work,
+                         int64_t work_bytes, void* stream);
+
 /* GMRES (lineax/_solver/gmres.py:106-413), restart <= 128.  Host sequence per
  * outer iteration (parity p): unless first pass, lxgb_gmres_cycle_begin(r),
  * then for kk < restart: w = M A V[kk] (V[kk] of right-hand side c at work +

@@ -1,8 +1,8 @@
 """lineax_gb300 — a GB300 (sm_103a) solve engine behind lineax's solver API.
 
 The public names mirror lineax/__init__.py for the hot path: ``linear_solve``
-with the ``LU``, ``Cholesky``, ``QR``, ``Triangular``, ``CG`` and ``GMRES``
-solvers over ``MatrixLinearOperator`` / ``FunctionLinearOperator``, the tags,
+with the ``LU``, ``Cholesky``, ``QR``, ``Triangular``, ``CG``, ``GMRES`` and
+``BiCGStab`` solvers over ``MatrixLinearOperator`` / ``FunctionLinearOperator``, the tags,
 ``RESULTS`` and ``Solution``.  Vectors and matrices are CUDA torch tensors; all
 arithmetic runs in the hand-written kernels of liblxgb.so (C ABI in
 include/lxgb.h).  There is no CPU fallback: without the built library or a GPU
@@ -29,7 +29,7 @@ from ._operator import (
 )
 from ._solution import RESULTS, LinearSolveError, Solution
 from ._solve import AbstractLinearSolver, AutoLinearSolver, invert, linear_solve
-from ._solver import CG, GMRES, LU, QR, Cholesky, Diagonal, Triangular
+from ._solver import CG, GMRES, LU, QR, BiCGStab, Cholesky, Diagonal, Triangular
 from ._structure import ShapeDtypeStruct
 from ._tags import (
     diagonal_tag,

@@ -61,6 +61,15 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         ctypes.c_int,
         [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i32, c_i64, c_i32, c_f64, c_f64, c_p, c_i64, c_p]),
     "lxgb_cg_status": (ctypes.c_int, [c_i32, c_i64, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_bicgstab_workspace_size": (c_i64, [c_i32, c_i64]),
+    "lxgb_bicgstab_start": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i64, c_i32, c_p,
+                                           c_i64, c_p]),
+    "lxgb_bicgstab_direction": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_i64,
+                                               c_p]),
+    "lxgb_bicgstab_s": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_bicgstab_update": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p,
+                                            c_f64, c_f64, c_i64, c_i32, c_p, c_i64, c_p]),
+    "lxgb_bicgstab_status": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_i64, c_p]),
     "lxgb_gmres_workspace_size": (c_i64, [c_i32, c_i64, c_i32]),
     "lxgb_gmres_basis_offset": (c_i64, [c_i32, c_i64, c_i32, c_i32]),
     "lxgb_gmres_init": (ctypes.c_int, [c_i32, c_i64, c_i32, c_p, c_i64, c_p]),

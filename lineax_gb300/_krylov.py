@@ -1,5 +1,5 @@
-"""Host drivers of the device Krylov solvers (CG, GMRES) for a block of k
-right-hand sides.
+"""Host drivers of the device Krylov solvers (CG, GMRES, BiCGStab) for a
+block of k right-hand sides.
 
 The loop structure restates lineax/_solver/cg.py:114-227 and
 lineax/_solver/gmres.py:106-413; every vector operation and reduction of the
@@ -266,6 +266,77 @@ def gmres_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_step
             res = BREAKDOWN
         results.append(res)
         steps.append(s)
+    return KrylovResult(y, steps, results)
+
+
+def bicgstab_block(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+                   preconditioner=None, y0: torch.Tensor | None = None) -> KrylovResult:
+    """BiCGStab (lineax/_solver/bicgstab.py:78-205) on the (k, n) block b,
+    right-preconditioned; every vector update and reduction in liblxgb.so
+    (lxgb_bicgstab_*), operator and preconditioner products here."""
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    k, n = b.shape
+    dev = b.device
+    max_steps_ = 10 * n if max_steps is None else int(max_steps)   # :82-88
+    has_scale = not (atol == 0 and rtol == 0)
+    pre = preconditioner
+    y = (torch.zeros_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone())
+    r = (b - block_mv(operator, y)).contiguous() if y0 is not None else b.clone()  # :105
+    r0 = torch.empty_like(b)
+    p = torch.empty_like(b)
+    v = torch.empty_like(b)
+    s_ = torch.empty_like(b)
+    wbytes = int(_ffi.load().lxgb_bicgstab_workspace_size(k, n))
+    work = _work(wbytes, dev)
+    wb = work.numel() * 8
+    st = _stream(dev)
+    _ffi.call("lxgb_bicgstab_start", k, n, _ffi.ptr(r), _ffi.ptr(r0), _ffi.ptr(p), _ffi.ptr(v),
+              max_steps_, int(has_scale), _ffi.ptr(work), wb, st)
+    steps_d = torch.empty(k, dtype=torch.int32, device=dev)
+    act_d = torch.empty(k, dtype=torch.int32, device=dev)
+    scal_d = torch.empty(3 * k, dtype=torch.float64, device=dev)
+    nc_d = torch.empty(k, dtype=torch.int32, device=dev)
+
+    def active():
+        _ffi.call("lxgb_bicgstab_status", k, n, 0, _ffi.ptr(act_d), 0, 0, _ffi.ptr(work), wb, st)
+        return act_d.cpu().tolist()
+
+    act = active()
+    it = 0
+    while any(act) and it < max_steps_:
+        _ffi.call("lxgb_bicgstab_direction", k, n, _ffi.ptr(r0), _ffi.ptr(r), _ffi.ptr(v),
+                  _ffi.ptr(p), _ffi.ptr(work), wb, st)
+        x = block_mv(pre, p).contiguous() if pre is not None else p
+        v = block_mv(operator, x).contiguous()
+        _ffi.call("lxgb_bicgstab_s", k, n, _ffi.ptr(r0), _ffi.ptr(r), _ffi.ptr(v), _ffi.ptr(s_),
+                  _ffi.ptr(work), wb, st)
+        z = block_mv(pre, s_).contiguous() if pre is not None else s_
+        t = block_mv(operator, z).contiguous()
+        _ffi.call("lxgb_bicgstab_update", k, n, _ffi.ptr(x), _ffi.ptr(z), _ffi.ptr(s_),
+                  _ffi.ptr(t), _ffi.ptr(b), _ffi.ptr(y), _ffi.ptr(r), float(rtol), float(atol),
+                  max_steps_, int(has_scale), _ffi.ptr(work), wb, st)
+        if _check_schedule(it):
+            act = active()
+        it += 1
+    _ffi.call("lxgb_bicgstab_status", k, n, _ffi.ptr(steps_d), 0, _ffi.ptr(scal_d),
+              _ffi.ptr(nc_d), _ffi.ptr(work), wb, st)
+    steps = steps_d.cpu().tolist()
+    scal = scal_d.cpu().view(3, k).tolist()
+    ncs = nc_d.cpu().tolist()
+    results = []
+    for c in range(k):                                               # :188-202
+        if max_steps is None:
+            res = SINGULAR if steps[c] == max_steps_ else SUCCESSFUL
+        elif has_scale:
+            res = MAX_STEPS_REACHED if steps[c] == max_steps_ else SUCCESSFUL
+        else:
+            res = SUCCESSFUL
+        rho, alpha, omega = scal[0][c], scal[1][c], scal[2][c]
+        if (omega == 0.0 or alpha == 0.0 or rho == 0.0) and ncs[c]:
+            res = BREAKDOWN
+        results.append(res)
     return KrylovResult(y, steps, results)
 
 

@@ -17,5 +17,9 @@ try:
     from .gmres import GMRES
 except ImportError:  # pragma: no cover
     GMRES = None
+try:
+    from .bicgstab import BiCGStab
+except ImportError:  # pragma: no cover
+    BiCGStab = None
 
-__all__ = ["LU", "Cholesky", "QR", "Triangular", "CG", "GMRES", "Diagonal"]
+__all__ = ["LU", "Cholesky", "QR", "Triangular", "CG", "GMRES", "BiCGStab", "Diagonal"]

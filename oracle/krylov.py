@@ -1,4 +1,4 @@
-"""Statement-for-statement NumPy restatements of lineax's CG and GMRES.
+"""Statement-for-statement NumPy restatements of lineax's CG, GMRES and BiCGStab.
 
 Test infrastructure only (see oracle/__init__.py).  One right-hand side per
 call: under ``jax.vmap`` the reference evaluates every batch element exactly
@@ -221,6 +221,61 @@ def gmres(matvec, b, *, rtol, atol, norm=max_norm, max_steps=None, restart=20,
     if deferred and not_conv(r, diff, y):
         result = BREAKDOWN
     return y, result, num_steps
+
+
+def bicgstab(matvec, b, *, rtol, atol, norm=max_norm, max_steps=None, precond=None,
+             y0=None):
+    """lineax BiCGStab (lineax/_solver/bicgstab.py:78-205), right-preconditioned,
+    FP64 (the ``jax_enable_x64`` branch of the breakdown test, :107-113).
+    Returns (solution, result, num_steps)."""
+    b = np.asarray(b, np.float64)
+    pre = precond if precond is not None else (lambda v: v)
+    y0 = np.zeros_like(b) if y0 is None else np.asarray(y0, np.float64)
+    size = b.size
+    max_steps_ = 10 * size if max_steps is None else max_steps          # :82-88
+    b_scale = (atol + rtol * np.abs(b)) if _has_scale(rtol, atol) else None  # :89-96
+    r0 = b - matvec(y0)                                                  # :105
+
+    def breakdown_occurred(omega, alpha, rho):                          # :107-113
+        return omega == 0.0 or alpha == 0.0 or rho == 0.0
+
+    def not_converged(r, diff, y):                                       # :115-126
+        return _not_converged(r, diff, y, b_scale, rtol, atol, norm)
+
+    y, r = y0, r0
+    alpha = omega = rho = 1.0                                            # :171
+    p = np.zeros_like(b)
+    v = np.zeros_like(b)
+    diff = np.full_like(y0, np.inf)
+    step = 0
+    # cond_fun :128-133
+    while (not breakdown_occurred(omega, alpha, rho)) and not_converged(r, diff, y) \
+            and step < max_steps_:
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            rho_new = float(np.dot(r0, r))                               # :138
+            beta = (np.float64(rho_new) / np.float64(rho)) * (np.float64(alpha) / np.float64(omega))
+            p = r + beta * (p - omega * v)                               # :140
+            x = pre(p)                                                   # :144
+            v = matvec(x)
+            alpha = float(np.float64(rho_new) / np.float64(np.dot(r0, v)))  # :147
+            s = r - alpha * v
+            z = pre(s)                                                   # :150
+            t = matvec(z)
+            omega = float(np.float64(np.dot(s, t)) / np.float64(np.dot(t, t)))  # :153
+            diff = alpha * x + omega * z                                 # :155
+            y = y + diff
+            r = s - omega * t
+        rho = rho_new
+        step += 1
+    if max_steps is None:                                                # :188-197
+        result = SINGULAR if step == max_steps_ else SUCCESSFUL
+    elif b_scale is not None:
+        result = MAX_STEPS_REACHED if step == max_steps_ else SUCCESSFUL
+    else:
+        result = SUCCESSFUL
+    if breakdown_occurred(omega, alpha, rho) and not_converged(r, diff, y):  # :199-202
+        result = BREAKDOWN
+    return y, result, step
 
 
 def finalize_result(x, result, b) -> int:

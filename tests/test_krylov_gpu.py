@@ -1,4 +1,4 @@
-"""GPU parity: CG and GMRES (device Krylov engine) against the NumPy
+"""GPU parity: CG, GMRES and BiCGStab (device Krylov engine) against the NumPy
 restatements of lineax's loops, including the reference's failure case."""
 
 import json
@@ -200,3 +200,88 @@ def test_cg_mixed_precision_poisson(dev, nx, ny, k):
     assert sol.result == lx.RESULTS.successful
     capped = _krylov.cg_poisson_mixed(op, t(b, dev), rtol=1e-10, atol=1e-10, max_steps=16)
     assert all(s == 16 for s in capped.steps) and all(r_ == 1 for r_ in capped.results)
+
+
+def nonsym(rng, n, shift=2.0):
+    return rng.standard_normal((n, n)) / np.sqrt(n) + shift * np.eye(n)
+
+
+@pytest.mark.parametrize("n,tol", [(10, 1e-10), (60, 1e-10), (150, 1e-12)])
+def test_bicgstab_matches_oracle(dev, n, tol):
+    rng = np.random.default_rng(100 + n)
+    a = nonsym(rng, n)
+    b = rng.standard_normal(n)
+    op = lx.MatrixLinearOperator(t(a, dev))
+    sol = lx.linear_solve(op, t(b, dev), lx.BiCGStab(rtol=tol, atol=tol))
+    x_ref, res_ref, steps_ref = krylov.bicgstab(lambda v: a @ v, b, rtol=tol, atol=tol)
+    assert sol.result == res_ref == 0
+    assert abs(sol.stats["num_steps"] - steps_ref) <= 1
+    np.testing.assert_allclose(sol.value.cpu().numpy(), x_ref, rtol=1e-8, atol=1e-10)
+    assert dense.backward_error(a, sol.value.cpu().numpy(), b) < 1e-9
+
+
+def test_bicgstab_max_steps_only(dev):
+    """tests/test_solve.py::test_iterative_solver_max_steps_only (BiCGStab
+    leg): NSD-tagged 1-D Poisson, rtol = atol = 0, max_steps = 2."""
+    n = 100
+    p = -2 * np.eye(n) + np.eye(n, k=1) + np.eye(n, k=-1)
+    b = np.random.default_rng(0).standard_normal(n)
+    op = lx.MatrixLinearOperator(t(p, dev), (lx.negative_semidefinite_tag, lx.symmetric_tag))
+    sol = lx.linear_solve(op, t(b, dev), lx.BiCGStab(0.0, 0.0, max_steps=2))
+    x_ref, res_ref, steps_ref = krylov.bicgstab(lambda v: p @ v, b, rtol=0.0, atol=0.0,
+                                                max_steps=2)
+    assert sol.stats["num_steps"] == steps_ref == 2 and sol.result == res_ref
+    np.testing.assert_allclose(sol.value.cpu().numpy(), x_ref, rtol=1e-10, atol=1e-12)
+
+
+def test_bicgstab_preconditioned_block_equals_alone(dev):
+    rng = np.random.default_rng(14)
+    n, k = 120, 3
+    a = rng.standard_normal((n, n)) / np.sqrt(n) + np.diag(np.linspace(1, 10, n))
+    m = np.diag(1.0 / np.diag(a))
+    b = rng.standard_normal((k, n))
+    op = lx.MatrixLinearOperator(t(a, dev))
+    pre = lx.MatrixLinearOperator(t(m, dev))
+    res = _krylov.bicgstab_block(op, t(b, dev), rtol=1e-10, atol=1e-10, preconditioner=pre)
+    for c in range(k):
+        x_ref, r_ref, s_ref = krylov.bicgstab(lambda v: a @ v, b[c], rtol=1e-10, atol=1e-10,
+                                              precond=lambda v: m @ v)
+        assert res.results[c] == r_ref and abs(res.steps[c] - s_ref) <= 1
+        np.testing.assert_allclose(res.y[c].cpu().numpy(), x_ref, rtol=1e-7, atol=1e-9)
+        alone = _krylov.bicgstab_block(op, t(b[c:c + 1], dev), rtol=1e-10, atol=1e-10,
+                                       preconditioner=pre)
+        assert torch.equal(alone.y[0], res.y[c]) and alone.steps[0] == res.steps[c]
+
+
+def test_bicgstab_y0_and_transpose(dev):
+    rng = np.random.default_rng(15)
+    n = 80
+    a = nonsym(rng, n)
+    b = rng.standard_normal(n)
+    y0 = rng.standard_normal(n)
+    op = lx.MatrixLinearOperator(t(a, dev))
+    sol = lx.linear_solve(op, t(b, dev), lx.BiCGStab(1e-11, 1e-11), options={"y0": t(y0, dev)})
+    x_ref, r_ref, s_ref = krylov.bicgstab(lambda v: a @ v, b, rtol=1e-11, atol=1e-11, y0=y0)
+    assert sol.result == r_ref == 0 and abs(sol.stats["num_steps"] - s_ref) <= 1
+    np.testing.assert_allclose(sol.value.cpu().numpy(), x_ref, rtol=1e-8, atol=1e-10)
+    solver = lx.BiCGStab(1e-11, 1e-11)
+    state = solver.init(op, {})
+    tstate, topts = solver.transpose(state, {})
+    xt, rt, _ = solver.compute(tstate, t(b, dev), topts)
+    assert rt == 0
+    assert dense.backward_error(a.T, xt.cpu().numpy(), b) < 1e-9
+
+
+def test_bicgstab_singular_reports_failure(dev):
+    """A zero row (the reference's singular-matrix construction for Krylov
+    solvers): the solve does not report success, as in the oracle."""
+    rng = np.random.default_rng(16)
+    n = 30
+    a = nonsym(rng, n)
+    a[7] = 0.0
+    b = rng.standard_normal(n)
+    op = lx.MatrixLinearOperator(t(a, dev))
+    sol = lx.linear_solve(op, t(b, dev), lx.BiCGStab(1e-10, 1e-10), throw=False)
+    x_ref, r_ref, _ = krylov.bicgstab(lambda v: a @ v, b, rtol=1e-10, atol=1e-10)
+    assert krylov.finalize_result(x_ref, r_ref, b) != 0
+    assert sol.result != lx.RESULTS.successful

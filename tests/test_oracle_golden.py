@@ -90,3 +90,47 @@ def test_oracle_cg_max_steps_only_poisson():
     b = np.random.default_rng(0).standard_normal(n)
     x, result, steps = krylov.cg(lambda v: p @ v, b, rtol=0.0, atol=0.0, max_steps=2, nsd=True)
     assert steps == 2 and result == krylov.SUCCESSFUL
+
+
+def test_oracle_bicgstab_iterates_match_scipy():
+    """The BiCGStab restatement against an independent implementation of the
+    same published recurrence (SciPy's bicgstab, right-preconditioned): the
+    iterate after k steps agrees (no stopping test involved: tolerances 0)."""
+    from scipy.sparse.linalg import LinearOperator, bicgstab as sp_bicgstab
+
+    rng = np.random.default_rng(5)
+    n = 60
+    a = rng.standard_normal((n, n)) / np.sqrt(n) + 3 * np.eye(n)
+    b = rng.standard_normal(n)
+    d = np.diag(a).copy()
+    for k in (1, 3, 7):
+        for pre in (None, lambda v: v / d):
+            x, res, steps = krylov.bicgstab(lambda v: a @ v, b, rtol=0.0, atol=0.0, max_steps=k,
+                                            precond=pre)
+            m = None if pre is None else LinearOperator((n, n), matvec=pre)
+            xs, _ = sp_bicgstab(a, b, x0=np.zeros(n), rtol=0.0, atol=0.0, maxiter=k, M=m)
+            assert steps == k and res == krylov.SUCCESSFUL
+            np.testing.assert_allclose(x, xs, rtol=1e-10, atol=1e-12)
+
+
+def test_oracle_bicgstab_max_steps_only_poisson():
+    """tests/test_solve.py::test_iterative_solver_max_steps_only, BiCGStab leg."""
+    n = 100
+    p = -2 * np.eye(n) + np.eye(n, k=1) + np.eye(n, k=-1)
+    b = np.random.default_rng(0).standard_normal(n)
+    x, result, steps = krylov.bicgstab(lambda v: p @ v, b, rtol=0.0, atol=0.0, max_steps=2)
+    assert steps == 2 and result == krylov.SUCCESSFUL and np.all(np.isfinite(x))
+
+
+def test_oracle_bicgstab_converges_and_flags_singular():
+    rng = np.random.default_rng(1)
+    n = 40
+    a = rng.standard_normal((n, n)) / np.sqrt(n) + 2 * np.eye(n)
+    xt = rng.standard_normal(n)
+    x, result, _ = krylov.bicgstab(lambda v: a @ v, a @ xt, rtol=1e-10, atol=1e-10)
+    assert result == krylov.SUCCESSFUL
+    np.testing.assert_allclose(x, xt, rtol=1e-8, atol=1e-8)
+    a[3] = 0.0  # a zero row, as the reference's singular-matrix tests build
+    b = rng.standard_normal(n)
+    x, result, _ = krylov.bicgstab(lambda v: a @ v, b, rtol=1e-10, atol=1e-10)
+    assert krylov.finalize_result(x, result, b) != krylov.SUCCESSFUL
