@@ -88,13 +88,37 @@ int lxgb_getrs_batched_f64(int64_t batch, int32_t n, int32_t nrhs,
  * jax.scipy.linalg.cho_factor(lower=False)).  info[s] = 0, or k+1 when the
  * leading minor of order k+1 is not positive definite (LAPACK potrf), or -2
  * when n[s] > max_n; a failed system's factor is unspecified.
- * Systems are taken from a work queue in index order, so placing the largest
- * first balances the launch.
+ * CTAs take the systems round-robin (system s by CTA s mod grid), so placing
+ * the largest first balances the launch.
  * Replaces jax.scipy.linalg.cho_factor(lower=False) at
  * lineax/_solver/cholesky.py:60. */
 int lxgb_potrf_ragged_f64(int64_t batch, int32_t max_n, const int32_t* n,
                           const int64_t* a_off, double* a, int32_t* info,
                           void* stream);
+
+/* Upper Cholesky A = Uᵀ U of one n×n SPD matrix (row stride lda), in place,
+ * on many CTAs: 64-row block rows, the diagonal block by one CTA, the block
+ * row by column-parallel substitution, the trailing matrix by
+ * lxgb_syrk_f64's update.  Every element receives the same FMA chain as in
+ * lxgb_potrf_ragged_f64, so the two return the same bits; the strictly lower
+ * triangle is zeroed.  *info (device) = 0, or k+1 for the first pivot that is
+ * not positive (the factor is then unspecified).  Replaces
+ * jax.scipy.linalg.cho_factor(lower=False) at lineax/_solver/cholesky.py:60
+ * for one large matrix. */
+int lxgb_potrf_f64(int64_t n, double* a, int64_t lda, int32_t* info,
+                   void* stream);
+
+/* Symmetric rank-k product, FP64, on the upper triangle of the n×n C (row
+ * stride ldc): S = AᵀA (trans 0, A k×n) or S = AAᵀ (trans 1, A n×k), A
+ * row-major with row stride lda.  update 0: C = S, and with fill = 1 the
+ * lower triangle receives the mirror (a full symmetric Gram matrix, the
+ * materialised normal-equations operator of lineax/_solver/normal.py:112-118);
+ * update 1: C -= S on j >= i, each element continuing its FMA chain from its
+ * stored value in k order (the Cholesky trailing update).  fill requires
+ * update 0. */
+int lxgb_syrk_f64(int32_t trans, int64_t n, int64_t k, const double* a,
+                  int64_t lda, int32_t update, double* c, int64_t ldc,
+                  int32_t fill, void* stream);
 
 /* Solve (Uᵀ U) X = B in place on B for each system of a ragged batch; system
  * s has nrhs[s] vectors of length n[s] starting at b + b_off[s].

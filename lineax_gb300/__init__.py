@@ -2,7 +2,7 @@
 
 The public names mirror lineax/__init__.py for the hot path: ``linear_solve``
 with the ``LU``, ``Cholesky``, ``QR``, ``Triangular``, ``CG``, ``GMRES`` and
-``BiCGStab`` solvers over ``MatrixLinearOperator`` / ``FunctionLinearOperator``, the tags,
+``BiCGStab`` solvers and the ``Normal`` wrapper over ``MatrixLinearOperator`` / ``FunctionLinearOperator``, the tags,
 ``RESULTS`` and ``Solution``.  Vectors and matrices are CUDA torch tensors; all
 arithmetic runs in the hand-written kernels of liblxgb.so (C ABI in
 include/lxgb.h).  There is no CPU fallback: without the built library or a GPU
@@ -12,10 +12,12 @@ the solvers raise.
 from ._norm import max_norm, rms_norm, sum_squares, tree_dot, two_norm
 from ._operator import (
     AbstractLinearOperator,
+    ComposedLinearOperator,
     FunctionLinearOperator,
     IdentityLinearOperator,
     MatrixLinearOperator,
     Poisson2DOperator,
+    TaggedLinearOperator,
     has_unit_diagonal,
     is_diagonal,
     is_lower_triangular,
@@ -29,7 +31,7 @@ from ._operator import (
 )
 from ._solution import RESULTS, LinearSolveError, Solution
 from ._solve import AbstractLinearSolver, AutoLinearSolver, invert, linear_solve
-from ._solver import CG, GMRES, LU, QR, BiCGStab, Cholesky, Diagonal, Triangular
+from ._solver import CG, GMRES, LU, QR, BiCGStab, Cholesky, Diagonal, Normal, Triangular
 from ._structure import ShapeDtypeStruct
 from ._tags import (
     diagonal_tag,

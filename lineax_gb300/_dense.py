@@ -79,6 +79,23 @@ def _one_system_meta(n: int, nrhs: int, device):
             offs[1:2].to(device))
 
 
+# Largest order factored by the one-CTA kernel (in shared memory); larger
+# matrices use the multi-CTA lxgb_potrf_f64.
+POTRF_ONE_CTA_MAX = 160
+
+
+def gram(a: torch.Tensor, tall: bool) -> torch.Tensor:
+    """AᵀA (tall) or AAᵀ (wide) of the row-major FP64 matrix a, full and
+    symmetric (lxgb_syrk_f64)."""
+    a = as_f64(a).contiguous()
+    m, n = a.shape
+    order = n if tall else m
+    c = torch.empty(order, order, dtype=torch.float64, device=a.device)
+    _ffi.call("lxgb_syrk_f64", 0 if tall else 1, order, m if tall else n, _ffi.ptr(a), n, 0,
+              _ffi.ptr(c), order, 1, _stream(a))
+    return c
+
+
 def cho_factor(a: torch.Tensor, negate: bool = False) -> torch.Tensor:
     """Upper U with (±)A = Uᵀ U, zeros below the diagonal; NaNs if the matrix
     is not positive definite (jax.lax.linalg.cholesky's failure value)."""
@@ -86,10 +103,14 @@ def cho_factor(a: torch.Tensor, negate: bool = False) -> torch.Tensor:
     if negate:
         u.neg_()
     n = u.shape[0]
-    nvec, _, aoff, _ = _one_system_meta(n, 1, u.device)
     info = torch.empty(1, dtype=torch.int32, device=u.device)
-    _ffi.call("lxgb_potrf_ragged_f64", 1, n, _ffi.ptr(nvec), _ffi.ptr(aoff), _ffi.ptr(u),
-              _ffi.ptr(info), _stream(u))
+    if n > POTRF_ONE_CTA_MAX:
+        # many CTAs (same bits as the one-CTA kernel)
+        _ffi.call("lxgb_potrf_f64", n, _ffi.ptr(u), n, _ffi.ptr(info), _stream(u))
+    else:
+        nvec, _, aoff, _ = _one_system_meta(n, 1, u.device)
+        _ffi.call("lxgb_potrf_ragged_f64", 1, n, _ffi.ptr(nvec), _ffi.ptr(aoff), _ffi.ptr(u),
+                  _ffi.ptr(info), _stream(u))
     # A failed factorisation is reported like jax: a NaN factor, which the
     # solve turns into RESULTS.singular.
     u.masked_fill_((info != 0).reshape(1, 1), float("nan"))

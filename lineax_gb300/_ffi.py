@@ -32,6 +32,9 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i64, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_i64, c_i32, c_p],
     ),
     "lxgb_potrf_ragged_f64": (ctypes.c_int, [c_i64, c_i32, c_p, c_p, c_p, c_p, c_p]),
+    "lxgb_potrf_f64": (ctypes.c_int, [c_i64, c_p, c_i64, c_p, c_p]),
+    "lxgb_syrk_f64": (ctypes.c_int, [c_i32, c_i64, c_i64, c_p, c_i64, c_i32, c_p, c_i64, c_i32,
+                                     c_p]),
     "lxgb_potrs_ragged_f64": (ctypes.c_int, [c_i64, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p]),
     "lxgb_posv_ragged_mixed_workspace_size": (c_i64, [c_i64, c_i32, c_i32]),
     "lxgb_posv_ragged_mixed": (

@@ -75,6 +75,9 @@ class AbstractLinearOperator(abc.ABC):
     def __neg__(self) -> "AbstractLinearOperator":
         return NegLinearOperator(self)
 
+    def __matmul__(self, other: "AbstractLinearOperator") -> "AbstractLinearOperator":
+        return ComposedLinearOperator(self, other)
+
 
 class MatrixLinearOperator(AbstractLinearOperator):
     """Wraps a 2-D tensor (lineax/_operator.py:232-285).  Vectors are 1-D."""
@@ -192,6 +195,65 @@ class NegLinearOperator(AbstractLinearOperator):
 
     def transpose(self):
         return NegLinearOperator(self.operator.transpose())
+
+    def in_structure(self):
+        return self.operator.in_structure()
+
+    def out_structure(self):
+        return self.operator.out_structure()
+
+
+class ComposedLinearOperator(AbstractLinearOperator):
+    """outer @ inner: x -> outer.mv(inner.mv(x)) (lineax/_operator.py's
+    ComposedLinearOperator).  `mv_block` applies both factors to a (k, n)
+    block, so Krylov solvers iterate on the composition block-wise."""
+
+    def __init__(self, outer: AbstractLinearOperator, inner: AbstractLinearOperator, tags=()):
+        self.outer, self.inner = outer, inner
+        self.tags = _frozenset(tags)
+
+    def mv(self, vector):
+        return self.outer.mv(self.inner.mv(vector))
+
+    def mv_block(self, x):
+        from ._krylov import block_mv
+
+        return block_mv(self.outer, block_mv(self.inner, x))
+
+    def as_matrix(self):
+        return materialise(self).matrix
+
+    def transpose(self):
+        return ComposedLinearOperator(self.inner.transpose(), self.outer.transpose(),
+                                      transpose_tags(self.tags))
+
+    def in_structure(self):
+        return self.inner.in_structure()
+
+    def out_structure(self):
+        return self.outer.out_structure()
+
+
+class TaggedLinearOperator(AbstractLinearOperator):
+    """An operator with extra tags (lineax/_operator.py's TaggedLinearOperator)."""
+
+    def __init__(self, operator: AbstractLinearOperator, tags):
+        self.operator = operator
+        self.tags = _frozenset(tags) | frozenset(operator.tags)
+
+    def mv(self, vector):
+        return self.operator.mv(vector)
+
+    def mv_block(self, x):
+        from ._krylov import block_mv
+
+        return block_mv(self.operator, x)
+
+    def as_matrix(self):
+        return self.operator.as_matrix()
+
+    def transpose(self):
+        return TaggedLinearOperator(self.operator.transpose(), transpose_tags(self.tags))
 
     def in_structure(self):
         return self.operator.in_structure()

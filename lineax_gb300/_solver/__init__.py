@@ -21,5 +21,7 @@ try:
     from .bicgstab import BiCGStab
 except ImportError:  # pragma: no cover
     BiCGStab = None
+from .normal import Normal
 
-__all__ = ["LU", "Cholesky", "QR", "Triangular", "CG", "GMRES", "BiCGStab", "Diagonal"]
+__all__ = ["LU", "Cholesky", "QR", "Triangular", "CG", "GMRES", "BiCGStab", "Normal",
+           "Diagonal"]

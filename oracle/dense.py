@@ -104,6 +104,18 @@ def qr_linear_solve(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 # ---------------------------------------------------------------------------
 # Triangular — lineax/_solver/triangular.py:49-85
 # ---------------------------------------------------------------------------
+def normal_linear_solve(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """lineax Normal(Cholesky()) (lineax/_solver/normal.py:102-136): the
+    Cholesky solve of AᵀA x = Aᵀb when A is tall (m >= n), else of
+    A Aᵀ y = b followed by x = Aᵀ y; FP64 LAPACK."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m, n = a.shape
+    if m >= n:
+        return cholesky_linear_solve(a.T @ a, a.T @ b)
+    return a.T @ cholesky_linear_solve(a @ a.T, b)
+
+
 def triangular_solve(t, b, lower: bool, unit_diagonal: bool, transpose: bool = False):
     """solve_triangular(matrix, b, trans, lower, unit_diagonal) at triangular.py:81."""
     return sl.solve_triangular(
