@@ -648,7 +648,8 @@ def run_qr_ls(args):
     out = {"workload": f"qr_least_squares_{m}x{n}", "metric": "least-squares solves/s",
            "unit": "solves/s"}
     xref = None
-    for name, solver in (("fp64", lx.QR()), ("mixed", lx.QR(precision="mixed"))):
+    for name, solver in (("fp64", lx.QR()), ("mixed", lx.QR(precision="mixed")),
+                         ("normal_cholesky", lx.Normal(lx.Cholesky()))):
         def step():
             return lx.linear_solve(op, b, solver).value
 
@@ -674,7 +675,11 @@ def run_qr_ls(args):
                           "frac": flops / (ms * 1e-3) / 1e12 / _fp64_peak()}
                          if name == "fp64" else
                          {"bound": "tensor (TF32 updates)", "effective_tflops":
-                          flops / (ms * 1e-3) / 1e12})}
+                          flops / (ms * 1e-3) / 1e12} if name == "mixed" else
+                         {"bound": "fp64 (Gram m n² + Cholesky n³/3)",
+                          "achieved": (m * n * n + n ** 3 / 3) / (ms * 1e-3) / 1e12,
+                          "peak": _fp64_peak(), "unit": "TFLOP/s",
+                          "frac": (m * n * n + n ** 3 / 3) / (ms * 1e-3) / 1e12 / _fp64_peak()})}
     out["value"] = out["mixed"]["solves_per_s"]
     if not args.no_cpu:
         import scipy.linalg as sl
@@ -690,6 +695,59 @@ def run_qr_ls(args):
                                "kind": "port", "sample": f"SciPy LAPACK economic QR + "
                                f"triangular solve of the same {m}×{n} problem, {reps} "
                                "repetitions"}
+    out["steps"], out["warmup"] = args.steps, args.warmup
+    print(json.dumps(out), flush=True)
+
+
+def run_cholesky_large(args):
+    """FP64 Cholesky solves of single large SPD matrices (A = G Gᵀ/n + I)
+    through lx.linear_solve(..., lx.Cholesky()): the multi-CTA factorisation
+    (lxgb_potrf_f64) plus the solve, and the factorisation alone."""
+    import torch
+
+    import lineax_gb300 as lx
+    from lineax_gb300 import _dense
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    g = torch.Generator(device=dev).manual_seed(4)
+    out = {"workload": "cholesky_large_f64", "metric": "factorisation ms", "unit": "ms",
+           "cases": []}
+    for n in (1024, 2048, 4096):
+        gm = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        a = gm @ gm.T / n + torch.eye(n, dtype=torch.float64, device=dev)
+        b = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+        op = lx.MatrixLinearOperator(a, lx.positive_semidefinite_tag)
+        case = {"n": n}
+        for name, fn in (("factor", lambda: _dense.cho_factor(a)),
+                         ("solve", lambda: lx.linear_solve(op, b, lx.Cholesky()).value)):
+            for _ in range(args.warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = _events(2)
+            e0.record()
+            for _ in range(args.steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            case[name + "_ms"] = e0.elapsed_time(e1) / args.steps
+        fl = n ** 3 / 3
+        case["roofline"] = {"bound": "fp64", "achieved": fl / (case["factor_ms"] * 1e-3) / 1e12,
+                            "peak": _fp64_peak(), "unit": "TFLOP/s",
+                            "frac": fl / (case["factor_ms"] * 1e-3) / 1e12 / _fp64_peak()}
+        x = lx.linear_solve(op, b, lx.Cholesky()).value
+        case["backward_error"] = float((b - a @ x).abs().max() /
+                                       (a.abs().sum(1).max() * x.abs().max() + b.abs().max()))
+        if not args.no_cpu:
+            import scipy.linalg as sl
+
+            ah = a.cpu().numpy()
+            cpu_s, reps = _cpu_time(lambda: sl.cho_factor(ah, lower=False), min_seconds=1.0,
+                                    max_reps=5)
+            case["cpu_baseline"] = {"value": cpu_s * 1e3, "unit": "ms", "cores": _host_cores(),
+                                    "kind": "port", "sample": f"SciPy LAPACK cho_factor of the "
+                                    f"same matrix, {reps} repetitions"}
+        out["cases"].append(case)
     out["steps"], out["warmup"] = args.steps, args.warmup
     print(json.dumps(out), flush=True)
 
@@ -931,7 +989,7 @@ def main():
                    help="systems per GPU (smaller values are for profiling runs only)")
     p.add_argument("--workload", default="ragged_cholesky",
                    choices=["ragged_cholesky", "gmres_ir", "lu_batch", "qr_ls", "cg_poisson",
-                            "serve", "peaks"],
+                            "serve", "peaks", "cholesky_large"],
                    help="gmres_ir: the dense mixed-precision LU + GMRES-IR workload")
     p.add_argument("--n", type=int, default=8192, help="order for --workload gmres_ir")
     p.add_argument("--restart", type=int, default=8, help="GMRES restart for --workload gmres_ir")
@@ -961,9 +1019,10 @@ def main():
     if args.workload == "gmres_ir":
         run_gmres_ir(args)
         return
-    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve", "peaks"):
+    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve", "peaks", "cholesky_large"):
         {"lu_batch": run_lu_batch, "qr_ls": run_qr_ls, "cg_poisson": run_cg_poisson,
-         "serve": run_serve, "peaks": run_peaks}[args.workload](args)
+         "serve": run_serve, "peaks": run_peaks,
+         "cholesky_large": run_cholesky_large}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -117,8 +117,19 @@ def cho_factor(a: torch.Tensor, negate: bool = False) -> torch.Tensor:
     return u
 
 
+# From this order on the Cholesky solve runs as two multi-CTA triangular
+# solves (lxgb_trsm_f64's blocked path) instead of the one-CTA potrs.
+POTRS_ONE_CTA_MAX = 767
+
+
 def cho_solve(u: torch.Tensor, b: torch.Tensor, negate: bool = False) -> torch.Tensor:
     n = u.shape[0]
+    if n > POTRS_ONE_CTA_MAX:
+        y = trsv(u, b, lower=False, trans=True, unit=False)     # Uᵀ y = b
+        x = trsv(u, y, lower=False, trans=False, unit=False)    # U x = y
+        if negate:
+            x.neg_()
+        return x
     x = as_f64(b).clone()
     nrhs = 1 if x.ndim == 1 else x.shape[0]
     nvec, nr, aoff, boff = _one_system_meta(n, nrhs, u.device)

@@ -107,7 +107,7 @@ def test_reference_kat_nonfinite_input(dev):
 @pytest.mark.parametrize("lower", [True, False])
 @pytest.mark.parametrize("unit", [True, False])
 @pytest.mark.parametrize("trans", [False, True])
-@pytest.mark.parametrize("n", [1, 31, 70, 257])
+@pytest.mark.parametrize("n", [1, 31, 70, 257, 768, 1500])
 def test_triangular_all_flags(dev, lower, unit, trans, n):
     rng = np.random.default_rng(n + 10 * lower + 100 * unit)
     m = rng.standard_normal((n, n)) / np.sqrt(n) + 2 * np.eye(n)
@@ -127,7 +127,7 @@ def test_triangular_all_flags(dev, lower, unit, trans, n):
 
 
 @pytest.mark.parametrize("nsd", [False, True])
-@pytest.mark.parametrize("n", [1, 5, 64, 160, 161, 300])
+@pytest.mark.parametrize("n", [1, 5, 64, 160, 161, 300, 800, 1300])
 def test_cholesky_solver(dev, n, nsd):
     rng = np.random.default_rng(n)
     g = rng.standard_normal((n, n))
