@@ -392,14 +392,16 @@ def run_gpu(args):
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak,
-            # DRAM bytes per launch: the ncu capture of the 512-system case read
-            # + wrote 364.5 MB for 151.4 MB of algorithmic bytes; scaled to this
-            # launch by its algorithmic bytes (the refinement re-reads A).
-            "traffic": hbm_bytes * (364.5 / 151.4),
+            # DRAM bytes per launch from one ncu capture of this 4096-system
+            # launch: 3985.4 MB read + 1039.7 MB written (A is read by the
+            # FP32 copy and by each refinement residual; factor slices of
+            # large systems spill from L2); scaled by the algorithmic bytes
+            # when --systems changes the workload.
+            "traffic": 5025.0e6 * hbm_bytes / 1215167544.0,
             "kernel": "posv_mixed_kernel",
             "note": "HBM roofline of the algorithmic bytes (A read once, b, x); the kernel is "
-                    "latency-bound (barriers, instruction fetch, L2 latency; "
-                    "profiles/posv_mixed_kernel_ragged512.md), see compute",
+                    "latency-bound (barriers, shared-memory and FP latency at 16 warps per "
+                    "SM; profiles/posv_mixed_kernel_ragged4096.md), see compute",
             "compute": {"fp32_flops": fp32_flops, "fp64_flops": fp64_flops,
                         "fp32_tflops": fp32_flops / (ms * 1e-3) / 1e12,
                         "fp64_tflops": fp64_flops / (ms * 1e-3) / 1e12},
