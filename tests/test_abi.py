@@ -56,6 +56,9 @@ def test_empty_problems_are_no_ops(lib_built):
 
     assert _ffi.call("lxgb_getrf_batched_f64", 0, 5, 0, 25, 0, 5, 0, 0) == 0
     assert _ffi.call("lxgb_trsm_f64", 0, 3, 0, 0, 1, 0, 0, 0, 0) == 0
+    assert _ffi.call("lxgb_posv_ragged_mixed", 0, 16, 1, 0, 0, 0, 0, 0, 0, 0, 1e-12, 10, 0, 0, 0,
+                     0, 0, 0) == 0
+    assert _ffi.call("lxgb_syrk_f64", 0, 0, 5, 0, 5, 0, 0, 0, 0, 0) == 0
 
 
 def test_mixed_workspace_size_grows_with_n(lib_built):

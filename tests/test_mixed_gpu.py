@@ -159,3 +159,42 @@ def test_host_solver_chunked_copies_match_device_solve(dev, chunks, buffers):
         ref2 = batched.spd_solve_ragged_mixed(rb, tol=TOL)
         torch.cuda.synchronize()
         assert torch.equal(x_h, ref2.x.cpu())
+
+
+def test_mixed_edge_cases(dev):
+    """Empty systems, a system with no right-hand side, the largest order
+    (1024), a non-finite matrix (breakdown reported, NaN solution) and a
+    system above the caller's max_n (info = -2) in one ragged launch."""
+    from lineax_gb300 import _ffi
+
+    rng = np.random.default_rng(41)
+    ns = [0, 33, 1024, 20, 50]
+    ks = [0, 2, 1, 0, 3]
+    mats, rhs = make_ragged(rng, ns, ks)
+    mats[4] = mats[4].copy()
+    mats[4][7, 7] = np.nan
+    rb = to_batch(mats, rhs, dev)
+    res = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    torch.cuda.synchronize()
+    info = res.info.cpu().numpy()
+    berr = res.berr.cpu().numpy()
+    assert info[0] == 0 and berr[0] == 0.0
+    assert info[1] == 0 and info[2] == 0 and info[3] == 0
+    assert berr[1] <= TOL and berr[2] <= TOL
+    for s in (1, 2):
+        xs = rb.system_b(res.x, s).cpu().numpy()
+        for k in range(xs.shape[0]):
+            assert dense.backward_error(mats[s], xs[k], rhs[s][k]) <= TOL
+    assert info[4] > 0 and np.isnan(rb.system_b(res.x, 4).cpu().numpy()).all()
+    # a caller-side max_n below a system's order: that system gets info -2
+    out = batched.MixedResult(x=torch.empty_like(rb.b), info=torch.empty_like(res.info),
+                              iters=torch.empty_like(res.iters), berr=torch.empty_like(res.berr))
+    ws = batched.MixedWorkspace(rb.batch, 64, rb.max_nrhs, dev)
+    _ffi.call("lxgb_posv_ragged_mixed", rb.batch, 64, rb.max_nrhs, _ffi.ptr(rb.n),
+              _ffi.ptr(rb.nrhs), _ffi.ptr(rb.a_off), _ffi.ptr(rb.a), _ffi.ptr(rb.b_off),
+              _ffi.ptr(rb.b), _ffi.ptr(out.x), TOL, 10, _ffi.ptr(out.info), _ffi.ptr(out.iters),
+              _ffi.ptr(out.berr), _ffi.ptr(ws.buf), ws.nbytes, _ffi.stream_handle(dev))
+    torch.cuda.synchronize()
+    info2 = out.info.cpu().numpy()
+    assert info2[2] == -2 and info2[1] == 0 and info2[3] == 0 and info2[0] == 0
+    assert torch.equal(rb.system_b(out.x, 1), rb.system_b(res.x, 1))
