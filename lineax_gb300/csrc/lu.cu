@@ -97,10 +97,16 @@ getrf_small_kernel(int n, double* __restrict__ a, int64_t stride_a, int32_t* __r
       my_info = k + 1;
     }
     __syncthreads();
-    // rank-1 update of the trailing block; u(k,j) cached in registers.
+    // rank-1 update of the trailing block; u(k,j) cached in registers.  Only
+    // the 32-column chunks that hold trailing columns are visited (a
+    // warp-uniform break): a predicated-off FP64 instruction still occupies
+    // GB300's narrow FP64 pipe, and unrolling over all kSmallMax columns
+    // issued about three times the needed DFMAs at n = 128.
+    const int nchunk = (n - k - 1 + 31) >> 5;
     double u[(kSmallMax + 31) / 32];
 #pragma unroll
     for (int c = 0; c < (kSmallMax + 31) / 32; ++c) {
+      if (c >= nchunk) break;
       const int j = k + 1 + tx + 32 * c;
       u[c] = (j < n) ? A[k * ld + j] : 0.0;
     }
@@ -108,6 +114,7 @@ getrf_small_kernel(int n, double* __restrict__ a, int64_t stride_a, int32_t* __r
       const double l = A[i * ld + k];
 #pragma unroll
       for (int c = 0; c < (kSmallMax + 31) / 32; ++c) {
+        if (c >= nchunk) break;
         const int j = k + 1 + tx + 32 * c;
         if (j < n) A[i * ld + j] = fma(-l, u[c], A[i * ld + j]);
       }
