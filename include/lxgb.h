@@ -157,6 +157,16 @@ int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
                            int32_t* iters, double* berr, void* work,
                            int64_t work_bytes, void* stream);
 
+/* Tuning table of the mixed solve (no counterpart in the reference): the
+ * largest order whose FP32 factor is formed in shared memory; larger systems
+ * use a per-CTA slice of the workspace (through L2).  0 <= small_max <= 144,
+ * default 144.  The host sets it once at initialisation from its autotune
+ * table (lineax_gb300/autotune.py, per GPU model), before solves are issued;
+ * lxgb_posv_ragged_mixed_workspace_size follows the current value, and each
+ * solve call reads it once. */
+int lxgb_posv_mixed_set_small_max(int32_t small_max);
+int32_t lxgb_posv_mixed_small_max(void);
+
 /* Allocation-free form of lxgb_posv_ragged_mixed (no counterpart in the
  * reference).  It is for callers that cannot allocate device memory when they
  * solve — an XLA/JAX FFI handler, whose device memory belongs to XLA and where

@@ -17,7 +17,7 @@ import dataclasses
 
 import torch
 
-from . import _dense, _ffi
+from . import _dense, _ffi, autotune
 from ._blas import as_device_f64
 
 
@@ -140,6 +140,7 @@ class MixedWorkspace:
     (kept by the serving loop and by CUDA-graph captures)."""
 
     def __init__(self, batch: int, max_n: int, max_nrhs: int, device="cuda"):
+        autotune.ensure_applied(device)
         nbytes = _ffi.load().lxgb_posv_ragged_mixed_workspace_size(batch, max_n, max_nrhs)
         self.nbytes = int(nbytes)
         # 256-byte alignment: torch's caching allocator returns 512-byte aligned blocks.
@@ -156,6 +157,7 @@ def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int
                            out: MixedResult | None = None) -> MixedResult:
     """FP32-factor / FP64-refined solve of every SPD system of the batch."""
     dev = batch.a.device
+    autotune.ensure_applied(dev)
     if workspace is None or not workspace.fits(batch.batch, batch.max_n, batch.max_nrhs):
         workspace = MixedWorkspace(batch.batch, batch.max_n, batch.max_nrhs, dev)
     if out is None:

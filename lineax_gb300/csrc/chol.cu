@@ -10,6 +10,8 @@
 // it stays L2-resident while the CTA works on it.
 #include <float.h>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "df.cuh"
 #include "potrf.cuh"
@@ -129,7 +131,7 @@ potrs_ragged_f64_kernel(int64_t batch, int max_n, const int32_t* __restrict__ nv
 //    backward error is <= tol (its result is the same alone or in a batch).
 // ---------------------------------------------------------------------------
 constexpr int kMxThreads = 256;
-constexpr int kMxSmallN = 144;   // 144*145*4 B = 82 KB factor in shared memory
+constexpr int kMxSmallN = 144;   // 144*145*4 B = 82 KB factor in shared memory (the most)
 constexpr int kMxKc = 8;         // right-hand sides per refinement chunk
 constexpr int kMxNB = 32;        // block rows of the large path and of the solves
 constexpr int kMxMaxN = 1024;
@@ -892,7 +894,7 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
                   const double* __restrict__ b, double* __restrict__ x, double tol, int max_iter,
                   int32_t* __restrict__ info, int32_t* __restrict__ iters,
                   double* __restrict__ berr_out, int* queue, const int32_t* __restrict__ order,
-                  float* __restrict__ factor_ws) {
+                  float* __restrict__ factor_ws, int small_max) {
   extern __shared__ float smem_mx[];
   __shared__ MxSmem sm;
   const int tid = threadIdx.x;
@@ -911,7 +913,7 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
       continue;
     }
     const double* A = a + a_off[s];
-    const bool small = n <= kMxSmallN;
+    const bool small = n <= small_max;
     const int ld = small ? (n | 1) : ((n + 31) & ~31);
     const int ldmax = (max_n + 31) & ~31;
     float* F = small ? smem_mx : factor_ws + (int64_t)blockIdx.x * ldmax * ldmax;
@@ -957,12 +959,18 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
 
 __global__ void reset_queue_kernel(int* queue) { *queue = 0; }
 
-static size_t mixed_smem_bytes(int max_n, int max_nrhs) {
+// Tuning table of the mixed solve: the largest order factored in shared
+// memory (larger systems take the L2-slice path).  Set from the host's
+// autotune table at initialisation (lxgb_posv_mixed_set_small_max); each call
+// reads it once, and workspace sizes follow it.
+static std::atomic<int> g_mx_small_max{kMxSmallN};
+
+static size_t mixed_smem_bytes(int max_n, int max_nrhs, int small_max) {
   (void)max_nrhs;
-  const int ns = max_n < kMxSmallN ? max_n : kMxSmallN;
+  const int ns = max_n < small_max ? max_n : small_max;
   const size_t small = (size_t)ns * (ns | 1) * sizeof(float) + (size_t)3 * kMxKc * ns * sizeof(float);
   size_t large = (size_t)3 * kMxKc * max_n * sizeof(float);
-  if (max_n > kMxSmallN && large < sizeof(MxStage)) large = sizeof(MxStage);
+  if (max_n > small_max && large < sizeof(MxStage)) large = sizeof(MxStage);
   return small > large ? small : large;
 }
 
@@ -971,9 +979,9 @@ static size_t mixed_smem_bytes(int max_n, int max_nrhs) {
 // can exceed the shared-memory size.
 static int64_t mixed_order_bytes(int64_t batch) { return (batch * 4 + 255) & ~(int64_t)255; }
 
-static int64_t mixed_slice_bytes(int max_n) {
+static int64_t mixed_slice_bytes(int max_n, int small_max) {
   const int64_t ld = (max_n + 31) & ~31;
-  return (max_n > kMxSmallN) ? ld * ld * (int64_t)sizeof(float) : 0;
+  return (max_n > small_max) ? ld * ld * (int64_t)sizeof(float) : 0;
 }
 
 static int mixed_grid(int64_t batch) {
@@ -987,7 +995,7 @@ static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs
                         const int32_t* nrhs, const int64_t* a_off, const double* a,
                         const int64_t* b_off, const double* b, double* x, double tol,
                         int32_t max_iter, int32_t* info, int32_t* iters, double* berr,
-                        void* scratch, bool ordered, cudaStream_t st) {
+                        void* scratch, bool ordered, int small_max, cudaStream_t st) {
   char* base = reinterpret_cast<char*>(scratch);
   int* queue = reinterpret_cast<int*>(base);
   int32_t* order = ordered ? reinterpret_cast<int32_t*>(base + kQueueHeader) : nullptr;
@@ -997,12 +1005,12 @@ static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs
     order_systems_kernel<<<1, kOrderThreads, 0, st>>>(batch, n, order, queue);
   else
     reset_queue_kernel<<<1, 1, 0, st>>>(queue);
-  const size_t smem = mixed_smem_bytes(max_n, max_nrhs);
+  const size_t smem = mixed_smem_bytes(max_n, max_nrhs, small_max);
   LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(posv_mixed_kernel), (int)smem),
                 "posv_mixed: set smem");
   posv_mixed_kernel<<<(unsigned)grid, kMxThreads, smem, st>>>(
       batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
-      queue, order, factor_ws);
+      queue, order, factor_ws, small_max);
   return check_launch("posv_mixed");
 }
 
@@ -1044,13 +1052,26 @@ extern "C" int lxgb_potrs_ragged_f64(int64_t batch, int32_t max_n, const int32_t
   return check_launch("potrs ragged");
 }
 
+static int64_t mixed_workspace_bytes(int64_t batch, int32_t max_n, int small_max) {
+  if (batch <= 0 || max_n <= 0) return kQueueHeader;
+  return kQueueHeader + mixed_order_bytes(batch) +
+         (int64_t)mixed_grid(batch) * mixed_slice_bytes(max_n, small_max);
+}
+
 extern "C" int64_t lxgb_posv_ragged_mixed_workspace_size(int64_t batch, int32_t max_n,
                                                          int32_t max_nrhs) {
   (void)max_nrhs;
-  if (batch <= 0 || max_n <= 0) return kQueueHeader;
-  return kQueueHeader + mixed_order_bytes(batch) +
-         (int64_t)mixed_grid(batch) * mixed_slice_bytes(max_n);
+  return mixed_workspace_bytes(batch, max_n, g_mx_small_max.load());
 }
+
+extern "C" int lxgb_posv_mixed_set_small_max(int32_t small_max) {
+  LXGB_REQUIRE(small_max >= 0 && small_max <= kMxSmallN,
+               "posv_mixed: small_max must be in [0, 144]");
+  g_mx_small_max.store(small_max);
+  return LXGB_SUCCESSFUL;
+}
+
+extern "C" int32_t lxgb_posv_mixed_small_max(void) { return g_mx_small_max.load(); }
 
 extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
                                       const int32_t* n, const int32_t* nrhs, const int64_t* a_off,
@@ -1066,12 +1087,14 @@ extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_
   LXGB_REQUIRE(max_iter >= 1, "posv_mixed: max_iter must be >= 1");
   LXGB_REQUIRE(max_n <= kMxMaxN, "posv_mixed: max_n above 1024");
   LXGB_REQUIRE(((uintptr_t)work & 255) == 0, "posv_mixed: workspace must be 256-byte aligned");
-  if (work_bytes < lxgb_posv_ragged_mixed_workspace_size(batch, max_n, max_nrhs)) {
+  const int small_max = g_mx_small_max.load();
+  if (work_bytes < mixed_workspace_bytes(batch, max_n, small_max)) {
     set_last_error("posv_mixed: workspace too small");
     return LXGB_WORKSPACE_TOO_SMALL;
   }
   return mixed_launch(mixed_grid(batch), batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x,
-                      tol, max_iter, info, iters, berr, work, true, as_stream(stream));
+                      tol, max_iter, info, iters, berr, work, true, small_max,
+                      as_stream(stream));
 }
 
 // ---------------------------------------------------------------------------
@@ -1137,7 +1160,8 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
   // goes in what the slices leave over; without room for it systems go in
   // index order.
   int64_t grid = mixed_grid(batch);
-  const int64_t slice = mixed_slice_bytes(max_n);
+  const int small_max = g_mx_small_max.load();
+  const int64_t slice = mixed_slice_bytes(max_n, small_max);
   const int64_t room = (int64_t)LXGB_POSV_NOALLOC_SCRATCH_BYTES - kQueueHeader;
   if (slice > 0) {
     const int64_t slices = room / slice;
@@ -1156,5 +1180,6 @@ extern "C" int lxgb_posv_ragged_mixed_noalloc(int64_t batch, int32_t max_n, int3
   // mixed_launch clears the work-queue counter, which the array keeps from the
   // previous call.
   return mixed_launch((int)grid, batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol,
-                      max_iter, info, iters, berr, scratch, ordered, as_stream(stream));
+                      max_iter, info, iters, berr, scratch, ordered, small_max,
+                      as_stream(stream));
 }
