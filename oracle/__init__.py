@@ -3,8 +3,8 @@
 This package restates, on the CPU, what the reference lineax solvers compute,
 so that the GPU engine can be checked against it.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference arm
-may import it, and only as the checker or the timed CPU baseline — the GPU
-product path never calls into it.
+may import it, and only to check results or as the timed CPU baseline — the
+GPU product path never calls into it.
 
 * ``dense``  — LU / Cholesky / QR / triangular solves.  The reference reaches
   LAPACK getrf/getrs, potrf/potrs, geqrf/ormqr and trsm through
