@@ -85,6 +85,8 @@ class MatrixLinearOperator(AbstractLinearOperator):
     def __init__(self, matrix: torch.Tensor, tags=()):
         if not isinstance(matrix, torch.Tensor) or matrix.ndim != 2:
             raise ValueError("`MatrixLinearOperator(matrix=...)` should be 2-dimensional.")
+        if matrix.is_complex():
+            raise ValueError("complex dtypes are not supported by lineax_gb300")
         if not torch.is_floating_point(matrix):
             matrix = matrix.to(torch.get_default_dtype())
         self.matrix = matrix

@@ -216,6 +216,8 @@ def linear_solve(
     for x in leaves:
         if not isinstance(x, torch.Tensor):
             x = torch.as_tensor(x, device="cuda")
+        if x.is_complex():
+            raise ValueError("complex dtypes are not supported by lineax_gb300")
         if not torch.is_floating_point(x):
             x = x.to(torch.get_default_dtype())
         fixed.append(x)

@@ -93,3 +93,19 @@ def test_identity_operator_short_circuit():
     v = torch.arange(3.0, dtype=torch.float64)
     sol = lx.linear_solve(op, v)
     assert sol.value is v and sol.result == lx.RESULTS.successful
+
+
+def test_complex_inputs_are_rejected():
+    """Complex dtypes are out of scope: building an operator from a complex
+    matrix, or solving for a complex vector, raises instead of dropping the
+    imaginary part."""
+    import pytest
+    import torch
+
+    import lineax_gb300 as lx
+
+    with pytest.raises(ValueError, match="complex"):
+        lx.MatrixLinearOperator(torch.eye(3, dtype=torch.complex128))
+    op = lx.MatrixLinearOperator(torch.eye(3, dtype=torch.float64))
+    with pytest.raises(ValueError, match="complex"):
+        lx.linear_solve(op, torch.ones(3, dtype=torch.complex128), lx.LU())
