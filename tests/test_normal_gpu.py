@@ -148,3 +148,26 @@ def test_normal_transpose_reuses_state(dev):
     # Aᵀ y = c is wide: the minimum-norm solution
     y_ref = np.linalg.lstsq(a.T, c, rcond=None)[0]
     np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=1e-9, atol=1e-11)
+
+
+def test_normal_cg_with_preconditioner(dev):
+    """normal.py:17-37: the outer preconditioner M enters the inner CG as
+    M Mᵀ (tall) or Mᵀ M (wide, with y0 -> Mᵀ y0); the solution is the
+    least-squares / minimum-norm one either way."""
+    rng = np.random.default_rng(21)
+    for m, n in ((240, 90), (90, 240)):
+        a = rng.standard_normal((m, n)) / np.sqrt(max(m, n)) + np.eye(m, n)
+        b = rng.standard_normal(m)
+        if m >= n:  # a diagonal M of the unknowns' space
+            pre = lx.MatrixLinearOperator(t(np.diag(1.0 / (1.0 + rng.random(n))), dev))
+        else:       # a general M of the right-hand side's space
+            pre = lx.MatrixLinearOperator(t(rng.standard_normal((m, m)) * 0.01 + np.eye(m), dev))
+        opts = {"preconditioner": pre}
+        if m < n:
+            opts["y0"] = t(np.zeros(m), dev)
+        op = lx.MatrixLinearOperator(t(a, dev))
+        sol = lx.linear_solve(op, t(b, dev), lx.Normal(lx.CG(rtol=1e-12, atol=1e-12)),
+                              options=opts)
+        assert sol.result == lx.RESULTS.successful
+        x_ls = np.linalg.lstsq(a, b, rcond=None)[0]
+        np.testing.assert_allclose(sol.value.cpu().numpy(), x_ls, rtol=1e-7, atol=1e-9)
