@@ -95,6 +95,19 @@ def _time_bucket(n: int, small_max: int, dev, systems: int, reps: int) -> float:
     return e0.elapsed_time(e1) / reps
 
 
+def choose_small_max(timings: dict, buckets=BUCKETS) -> int:
+    """The largest bucket up to which (contiguously from FLOOR) the shared-
+    memory path is not slower; DEFAULT_SMALL_MAX when that is every bucket."""
+    small_max = FLOOR
+    for i, n in enumerate(buckets):
+        t = timings[n]
+        if t["shared_ms"] <= t["slice_ms"] and small_max == (buckets[i - 1] if i else FLOOR):
+            small_max = n
+    if small_max == buckets[-1]:
+        small_max = DEFAULT_SMALL_MAX
+    return small_max
+
+
 def tune(device=None, buckets=BUCKETS, systems: int = 608, reps: int = 5) -> dict:
     """Time the shared-memory and the slice path on uniform batches of each
     bucket's order; small_max = the largest bucket up to which the shared-
@@ -107,18 +120,14 @@ def tune(device=None, buckets=BUCKETS, systems: int = 608, reps: int = 5) -> dic
         torch.device(device)
     before = int(_ffi.load().lxgb_posv_mixed_small_max())
     timings = {}
-    small_max = FLOOR
     try:
-        for i, n in enumerate(buckets):
+        for n in buckets:
             t_smem = _time_bucket(n, DEFAULT_SMALL_MAX, dev, systems, reps)
             t_slice = _time_bucket(n, n - 1, dev, systems, reps)
             timings[n] = {"shared_ms": t_smem, "slice_ms": t_slice}
-            if t_smem <= t_slice and small_max == (buckets[i - 1] if i else FLOOR):
-                small_max = n
     finally:
         _ffi.call("lxgb_posv_mixed_set_small_max", before)
-    if small_max == buckets[-1]:
-        small_max = DEFAULT_SMALL_MAX
+    small_max = choose_small_max(timings, buckets)
     return {"posv_mixed_small_max": small_max,
             "measured": {str(n): v for n, v in timings.items()},
             "systems_per_bucket": systems, "nrhs": 4}

@@ -201,6 +201,22 @@ class CapturedMixedSolve:
         return self.out
 
 
+def chunk_bounds(sizes, chunks: int) -> list:
+    """Boundaries [0, b1, ..., len(sizes)] of at most `chunks` contiguous,
+    non-empty ranges of about equal total size (a range closes once the
+    running total reaches its share)."""
+    nb = len(sizes)
+    k = max(1, min(int(chunks), nb))
+    total = float(sum(sizes)) or 1.0
+    bounds, acc = [0], 0
+    for s, sz in enumerate(sizes):
+        acc += sz
+        if len(bounds) < k and acc >= total * len(bounds) / k and s + 1 < nb:
+            bounds.append(s + 1)
+    bounds.append(nb)
+    return bounds
+
+
 class _HostSet:
     """One set of device buffers of HostRaggedSPDSolver (matrices, right-hand
     sides, results), cut into chunks."""
@@ -216,16 +232,7 @@ class _HostSet:
             iters=torch.empty(nb, dtype=torch.int32, device=device),
             berr=torch.empty(nb, dtype=torch.float64, device=device),
         )
-        # chunk boundaries: contiguous system ranges of about equal bytes
-        k = max(1, min(int(chunks), nb))
-        sizes = [n * n + n * r for n, r in zip(n_list, nrhs_list)]
-        total = float(sum(sizes)) or 1.0
-        bounds, acc = [0], 0
-        for s_, sz in enumerate(sizes):
-            acc += sz
-            if len(bounds) < k and acc >= total * len(bounds) / k and s_ + 1 < nb:
-                bounds.append(s_ + 1)
-        bounds.append(nb)
+        bounds = chunk_bounds([n * n + n * r for n, r in zip(n_list, nrhs_list)], chunks)
         self.chunks = []
         for lo, hi in zip(bounds[:-1], bounds[1:]):
             a0, b0 = a_off[lo], b_off[lo]

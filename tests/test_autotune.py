@@ -71,3 +71,24 @@ def test_mixed_solve_correct_at_every_threshold(dev, small_max):
                 assert dense.backward_error(mats[s].numpy(), xs[k], rhs[s][k].numpy()) <= 1e-12
     finally:
         _ffi.call("lxgb_posv_mixed_set_small_max", before)
+
+
+def test_choose_small_max_rule():
+    b = (48, 64, 80)
+    fast = {"shared_ms": 1.0, "slice_ms": 2.0}
+    slow = {"shared_ms": 2.0, "slice_ms": 1.0}
+    assert autotune.choose_small_max({48: fast, 64: fast, 80: fast}, b) == \
+        autotune.DEFAULT_SMALL_MAX
+    assert autotune.choose_small_max({48: fast, 64: slow, 80: fast}, b) == 48
+    assert autotune.choose_small_max({48: slow, 64: fast, 80: fast}, b) == autotune.FLOOR
+    # ties keep shared memory
+    tie = {"shared_ms": 1.0, "slice_ms": 1.0}
+    assert autotune.choose_small_max({48: tie, 64: fast, 80: slow}, b) == 64
+
+
+def test_committed_gb300_entry_matches_its_measurements():
+    table = autotune.load_table()
+    for entry in table.values():
+        timings = {int(n): v for n, v in entry["measured"].items()}
+        buckets = tuple(sorted(timings))
+        assert autotune.choose_small_max(timings, buckets) == entry["posv_mixed_small_max"]

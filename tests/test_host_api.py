@@ -109,3 +109,15 @@ def test_complex_inputs_are_rejected():
     op = lx.MatrixLinearOperator(torch.eye(3, dtype=torch.float64))
     with pytest.raises(ValueError, match="complex"):
         lx.linear_solve(op, torch.ones(3, dtype=torch.complex128), lx.LU())
+
+
+def test_host_solver_chunk_bounds():
+    from lineax_gb300.batched import chunk_bounds
+
+    assert chunk_bounds([5, 5, 5, 5], 2) == [0, 2, 4]
+    assert chunk_bounds([5, 5, 5, 5], 1) == [0, 4]
+    assert chunk_bounds([5, 5], 8) == [0, 1, 2]          # at most one range per system
+    assert chunk_bounds([100, 1, 1, 1], 2) == [0, 1, 4]   # the large system closes a range
+    assert chunk_bounds([1] * 10, 3) == [0, 4, 7, 10]
+    b = chunk_bounds([3, 0, 7, 2, 9, 4, 4, 1], 4)
+    assert b[0] == 0 and b[-1] == 8 and all(x < y for x, y in zip(b, b[1:]))
