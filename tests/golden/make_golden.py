@@ -12,7 +12,10 @@ and assert on, and writes them to tests/golden/reference_kats.json:
   matrix and true_x on which GMRES(restart=2, rtol=atol=1e-10) must report a
   failure;
 * tests/test_solve.py::test_nonfinite_input — right-hand sides containing
-  inf/NaN must give RESULTS.nonfinite_input.
+  inf/NaN must give RESULTS.nonfinite_input;
+* tests/test_singular.py::test_nonsquare_pytree_operator1/2 — the literal
+  2×3 and 3×2 systems whose QR and Normal(Cholesky()) solutions must equal the
+  least-squares (minimum-norm) answer.
 
 The JAX reference cannot run here (no JAX), so these literal cases are the
 reference's own answers.  Run from the repository root:
@@ -100,6 +103,16 @@ def main(ref_root: pathlib.Path) -> dict:
         "solver": {"kind": "GMRES", "rtol": 1e-10, "atol": 1e-10, "restart": 2},
         "expect": "result != successful",
     }
+    for name, key in (("test_nonsquare_pytree_operator1", "nonsquare_wide_2x3"),
+                      ("test_nonsquare_pytree_operator2", "nonsquare_tall_3x2")):
+        a = _assigns(_function(t_sing, name))
+        kats[key] = {
+            "source": f"tests/test_singular.py::{name}",
+            "matrix": [[float(v) for v in row] for row in _literal(a["matrix"][0])],
+            "vector": [float(v) for v in _literal(a["y"][0])],
+            "expect": "the least-squares / minimum-norm solution (jnp.linalg.lstsq)",
+            "solvers": ["Auto(well_posed=None)", "QR", "Normal(Cholesky)"],
+        }
     fn = _function(t_solve, "test_nonfinite_input")
     vecs = [_literal(v) for v in _assigns(fn)["vector"]]
     kats["nonfinite_input"] = {

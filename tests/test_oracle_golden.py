@@ -134,3 +134,15 @@ def test_oracle_bicgstab_converges_and_flags_singular():
     b = rng.standard_normal(n)
     x, result, _ = krylov.bicgstab(lambda v: a @ v, b, rtol=1e-10, atol=1e-10)
     assert krylov.finalize_result(x, result, b) != krylov.SUCCESSFUL
+
+
+@pytest.mark.parametrize("name", ["nonsquare_wide_2x3", "nonsquare_tall_3x2"])
+def test_oracle_nonsquare_kats(name):
+    """tests/test_singular.py::test_nonsquare_pytree_operator1/2: QR and
+    Normal(Cholesky()) return the least-squares / minimum-norm solution."""
+    k = GOLD[name]
+    a = np.array(k["matrix"])
+    b = np.array(k["vector"])
+    expect = np.linalg.lstsq(a, b, rcond=None)[0]
+    np.testing.assert_allclose(dense.qr_linear_solve(a, b), expect, rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(dense.normal_linear_solve(a, b), expect, rtol=1e-10, atol=1e-12)
