@@ -146,3 +146,43 @@ def test_oracle_nonsquare_kats(name):
     expect = np.linalg.lstsq(a, b, rcond=None)[0]
     np.testing.assert_allclose(dense.qr_linear_solve(a, b), expect, rtol=1e-12, atol=1e-13)
     np.testing.assert_allclose(dense.normal_linear_solve(a, b), expect, rtol=1e-10, atol=1e-12)
+
+
+def test_oracle_cg_iterates_match_scipy():
+    """The CG restatement against SciPy's independent implementation of the
+    same preconditioned recurrence: equal iterates for k < stabilise_every
+    steps (lineax replaces the residual at step 10; tolerances 0)."""
+    from scipy.sparse.linalg import LinearOperator, cg as sp_cg
+
+    rng = np.random.default_rng(7)
+    n = 60
+    g = rng.standard_normal((n, n))
+    a = g @ g.T / n + 0.5 * np.eye(n)
+    b = rng.standard_normal(n)
+    d = np.diag(a).copy()
+    for k in (1, 4, 9):
+        for pre in (None, lambda v: v / d):
+            x, res, steps = krylov.cg(lambda v: a @ v, b, rtol=0.0, atol=0.0, max_steps=k,
+                                      precond=pre)
+            m = None if pre is None else LinearOperator((n, n), matvec=pre)
+            xs, _ = sp_cg(a, b, x0=np.zeros(n), rtol=0.0, atol=0.0, maxiter=k, M=m)
+            assert steps == k and res == krylov.SUCCESSFUL
+            np.testing.assert_allclose(x, xs, rtol=1e-10, atol=1e-12)
+
+
+def test_oracle_gmres_cycle_matches_scipy():
+    """One restart cycle of the GMRES restatement (after lineax's dummy first
+    pass) gives the Krylov minimiser that SciPy's GMRES returns after one
+    cycle of the same length."""
+    from scipy.sparse.linalg import gmres as sp_gmres
+
+    rng = np.random.default_rng(8)
+    n = 50
+    a = rng.standard_normal((n, n)) / np.sqrt(n) + 2 * np.eye(n)
+    b = rng.standard_normal(n)
+    for k in (3, 8, 20):
+        x, res, steps = krylov.gmres(lambda v: a @ v, b, rtol=0.0, atol=0.0, max_steps=2,
+                                     restart=k)
+        xs, _ = sp_gmres(a, b, x0=np.zeros(n), rtol=0.0, atol=0.0, restart=k, maxiter=1)
+        assert steps == 2 and res == krylov.SUCCESSFUL
+        np.testing.assert_allclose(x, xs, rtol=1e-9, atol=1e-11)
