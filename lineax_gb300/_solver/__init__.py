@@ -1,27 +1,14 @@
 """Solvers of the GPU engine (the lineax solver types on the hot path)."""
 
+from .bicgstab import BiCGStab
+from .cg import CG
 from .cholesky import Cholesky
 from .diagonal import Diagonal
+from .gmres import GMRES
 from .lu import LU
-from .triangular import Triangular
-
-try:  # solvers added as their kernels land
-    from .qr import QR
-except ImportError:  # pragma: no cover
-    QR = None
-try:
-    from .cg import CG
-except ImportError:  # pragma: no cover
-    CG = None
-try:
-    from .gmres import GMRES
-except ImportError:  # pragma: no cover
-    GMRES = None
-try:
-    from .bicgstab import BiCGStab
-except ImportError:  # pragma: no cover
-    BiCGStab = None
 from .normal import Normal
+from .qr import QR
+from .triangular import Triangular
 
 __all__ = ["LU", "Cholesky", "QR", "Triangular", "CG", "GMRES", "BiCGStab", "Normal",
            "Diagonal"]

@@ -125,7 +125,9 @@ def main(ref_root: pathlib.Path) -> dict:
 
 
 if __name__ == "__main__":
-    root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the lineax source tree>")
+    root = pathlib.Path(sys.argv[1])
     kats = main(root)
     out = HERE / "reference_kats.json"
     out.write_text(json.dumps(kats, indent=1, allow_nan=True) + "\n")

@@ -69,8 +69,19 @@ def test_noalloc_matches_workspace_entry_twice(dev):
         assert (got.berr.cpu().numpy() <= TOL).all()
 
 
-def test_noalloc_rejects_oversize():
+def test_noalloc_rejects_oversize(dev):
+    # Real device buffers of a small batch, so that the call could only ever
+    # touch valid memory even if the size check moved after a launch.
+    rb, _, _ = _case(dev)
+    out_x = torch.zeros_like(rb.b)
+    info = torch.zeros(rb.batch, dtype=torch.int32, device=dev)
+    iters = torch.zeros(rb.batch, dtype=torch.int32, device=dev)
+    berr = torch.zeros(rb.batch, dtype=torch.float64, device=dev)
     with pytest.raises(_ffi.LxgbError) as e:
-        _ffi.call("lxgb_posv_ragged_mixed_noalloc", 1, 4096, 1, 1, 1, 1, 1, 1, 1, 1, TOL, 10,
-                  1, 1, 1, 0)
+        _ffi.call("lxgb_posv_ragged_mixed_noalloc", rb.batch, 4096, rb.max_nrhs,
+                  _ffi.ptr(rb.n), _ffi.ptr(rb.nrhs), _ffi.ptr(rb.a_off), _ffi.ptr(rb.a),
+                  _ffi.ptr(rb.b_off), _ffi.ptr(rb.b), _ffi.ptr(out_x), TOL, 10,
+                  _ffi.ptr(info), _ffi.ptr(iters), _ffi.ptr(berr), _ffi.stream_handle(dev))
     assert e.value.status == 100
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0  # nothing was launched
