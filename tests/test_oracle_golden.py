@@ -186,3 +186,25 @@ def test_oracle_gmres_cycle_matches_scipy():
         xs, _ = sp_gmres(a, b, x0=np.zeros(n), rtol=0.0, atol=0.0, restart=k, maxiter=1)
         assert steps == 2 and res == krylov.SUCCESSFUL
         np.testing.assert_allclose(x, xs, rtol=1e-9, atol=1e-11)
+
+
+def test_residual_exact_against_rational_arithmetic():
+    """oracle.dense.residual_exact: B - X Aᵀ to within 2^-70 of |X||A|ᵀ,
+    checked against exact rational arithmetic on a small case with a wide
+    dynamic range (products that cancel in FP64)."""
+    from fractions import Fraction
+
+    rng = np.random.default_rng(5)
+    n, k = 24, 3
+    a = rng.standard_normal((n, n)) * np.exp2(rng.integers(-30, 30, (n, n)))
+    x = rng.standard_normal((k, n))
+    b = x @ a.T  # b close to A x, so the residual is all cancellation
+    r = dense.residual_exact(a, x, b)
+    scale = np.abs(x) @ np.abs(a).T
+    for c in range(k):
+        for i in range(n):
+            exact = Fraction(b[c, i]) - sum(Fraction(a[i, j]) * Fraction(x[c, j])
+                                            for j in range(n))
+            assert abs(Fraction(r[c, i]) - exact) <= Fraction(scale[c, i]) / 2 ** 70
+    be = dense.backward_errors_exact(a, x, b)
+    assert be.shape == (k,) and (be >= 0).all() and (be < 1e-15).all()
