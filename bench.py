@@ -413,7 +413,7 @@ def run_gpu(args):
             "kernel": "posv_mixed_kernel",
             "note": "HBM roofline of the algorithmic bytes (A read once, b, x); the kernel is "
                     "latency-bound (barriers, shared-memory and FP latency at 16 warps per "
-                    "SM; profiles/posv_mixed_kernel_ragged4096.md), see compute",
+                    "SM), see compute",
             "compute": {"fp32_flops": fp32_flops, "fp64_flops": fp64_flops,
                         "fp32_tflops": fp32_flops / (ms * 1e-3) / 1e12,
                         "fp64_tflops": fp64_flops / (ms * 1e-3) / 1e12},
@@ -422,6 +422,10 @@ def run_gpu(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if not args.no_serve and world == 1:
+        # the served mixed request stream against the plain FP64 server
+        # (the metric's stream), with its own clock record
+        line["serving"] = serve_suite(args, dev, loads=(0.5,))
     print(json.dumps(line), flush=True)
 
 
@@ -856,17 +860,21 @@ def run_cg_poisson(args):
     print(json.dumps(out), flush=True)
 
 
-def run_serve(args):
+SERVE_ROUTES = ("chol_ragged", "lu_small", "lu_mixed", "qr_mixed", "qr_f64", "lu_f64",
+                "chol_f64")
+
+
+def serve_suite(args, dev, loads=(0.25, 0.5, 0.75), emit=None):
     """Serving mix (50% LU / 30% Cholesky / 20% QR, n log-uniform [32, 4096],
     1-16 right-hand sides, 30% on a resident operator): saturation throughput
     of the mixed-precision server and of the plain FP64 server on the same
-    requests, then open-loop Poisson arrivals for p50/p99 latency."""
+    requests, then open-loop Poisson arrivals at fractions `loads` of each
+    server's saturation rate for p50/p99 latency.  Clocks are sampled over the
+    whole suite.  Returns a summary dict; `emit` receives each result line."""
     import torch
 
     from lineax_gb300 import serve
 
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
     count = args.serve_requests
     warm = serve.synthetic_requests(24, seed=99, nmax=1024)
 
@@ -892,25 +900,58 @@ def run_serve(args):
                 "rhs_per_s": sum(r.nrhs for r in reqs) / wall, "wall_s": wall,
                 "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
                 "max_berr": max(c.berr for c in out),
+                "all_berr_le_tol": all(c.berr <= TOL for c in out),
                 "fallbacks": sum(c.fallback for c in out),
                 "reused": sum(c.reused for c in out),
-                "routes": {k: sum(c.route == k for c in out)
-                           for k in ("chol_ragged", "lu_small", "lu_mixed", "lu_f64")}}
+                "routes": {k: sum(c.route == k for c in out) for k in SERVE_ROUTES
+                           if any(c.route == k for c in out)}}
 
-    for mode in ("mixed", "fp64"):
-        serve.SolveServer(dev, mode=mode).run(warm, realtime=False)
-    torch.cuda.synchronize()
+    emit = emit or (lambda obj: None)
     tag = f"serve_{count}req_n32-{args.serve_nmax}"
-    sat = {m: one(m, None, 5) for m in ("fp64", "mixed")}
-    for m in ("fp64", "mixed"):
-        print(json.dumps({"workload": tag, "phase": "saturation", **sat[m]}), flush=True)
-    print(json.dumps({"workload": tag, "phase": "speedup",
-                      "mixed_over_fp64_solves_per_s":
-                          sat["mixed"]["solves_per_s"] / sat["fp64"]["solves_per_s"]}),
-          flush=True)
+    with ClockSampler(dev.index or 0) as clk:
+        for mode in ("mixed", "fp64"):
+            serve.SolveServer(dev, mode=mode).run(warm, realtime=False)
+        torch.cuda.synchronize()
+        sat = {m: one(m, None, 5) for m in ("fp64", "mixed")}
+        for m in ("fp64", "mixed"):
+            emit({"workload": tag, "phase": "saturation", **sat[m]})
+        ratio = sat["mixed"]["solves_per_s"] / sat["fp64"]["solves_per_s"]
+        emit({"workload": tag, "phase": "speedup", "mixed_over_fp64_solves_per_s": ratio})
+        sweep = []
+        for m in ("fp64", "mixed"):
+            for frac in loads:
+                row = {"load": frac, **one(m, frac * sat[m]["solves_per_s"], 6)}
+                sweep.append(row)
+                emit({"workload": tag, "phase": "open_loop", **row})
+    keep = ("solves_per_s", "p50_ms", "p99_ms", "max_berr", "all_berr_le_tol", "fallbacks",
+            "reused", "routes", "streams")
+    return {
+        "workload": tag, "requests": count,
+        "mix": f"50% LU / 30% Cholesky / 20% QR, n log-uniform [32, {args.serve_nmax}], "
+               "1-16 RHS, 30% reuse",
+        "saturation": {m: {k: sat[m][k] for k in keep} for m in ("mixed", "fp64")},
+        "mixed_over_fp64_solves_per_s": ratio,
+        "open_loop": [{k: r[k] for k in ("mode", "load", "offered_rate", "solves_per_s",
+                                         "p50_ms", "p99_ms")} for r in sweep],
+        "clocks": clk.summary(),
+    }
+
+
+def run_serve(args):
+    """The serving suite alone, one JSON line per result, plus the SciPy
+    CPU baseline on the same request stream."""
+    import torch
+
+    from lineax_gb300 import serve
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    summary = serve_suite(args, dev, emit=lambda o: print(json.dumps(o), flush=True))
+    print(json.dumps({"workload": summary["workload"], "phase": "clocks",
+                      "clocks": summary["clocks"]}), flush=True)
     if not args.no_cpu:
         # the same request stream solved one request at a time on the host
-        # cores with SciPy LAPACK (Cholesky for SPD requests, LU otherwise)
+        # cores with SciPy LAPACK (Cholesky, QR or LU as the request asks)
         import scipy.linalg as sl
 
         reqs = serve.synthetic_requests(60, seed=5, nmax=args.serve_nmax)
@@ -922,20 +963,19 @@ def run_serve(args):
                 bb = r.b.numpy().T
                 if r.kind == "cholesky":
                     sl.cho_solve(sl.cho_factor(a), bb)
+                elif r.kind == "qr":
+                    q, rr = sl.qr(a)
+                    sl.solve_triangular(rr, q.T @ bb)
                 else:
                     sl.lu_solve(sl.lu_factor(a), bb)
 
         cpu_s, reps = _cpu_time(cpu_stream, min_seconds=1.0, max_reps=2)
-        print(json.dumps({"workload": tag, "phase": "cpu_baseline", "value": len(reqs) / cpu_s,
-                          "unit": "solves/s", "cores": _host_cores(), "kind": "port",
+        print(json.dumps({"workload": summary["workload"], "phase": "cpu_baseline",
+                          "value": len(reqs) / cpu_s, "unit": "solves/s",
+                          "cores": _host_cores(), "kind": "port",
                           "sample": "the first 60 requests of the stream (no resident "
                                     "factors), SciPy LAPACK, one request at a time"}),
               flush=True)
-    # open-loop rate sweep: fractions of each server's saturation throughput
-    for m in ("fp64", "mixed"):
-        for frac in (0.25, 0.5, 0.75):
-            print(json.dumps({"workload": tag, "phase": "open_loop", "load": frac,
-                              **one(m, frac * sat[m]["solves_per_s"], 6)}), flush=True)
 
 
 def run_peaks(args):
@@ -999,6 +1039,8 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline measurement")
+    p.add_argument("--no-serve", action="store_true",
+                   help="skip the serving suite in the default line")
     p.add_argument("--systems", type=int, default=COUNT,
                    help="systems per GPU (smaller values are for profiling runs only)")
     p.add_argument("--workload", default="ragged_cholesky",

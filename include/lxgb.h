@@ -157,6 +157,27 @@ int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
                            int32_t* iters, double* berr, void* work,
                            int64_t work_bytes, void* stream);
 
+/* lxgb_posv_ragged_mixed with the FP32 factors kept between calls: the
+ * factor state a lineax solver returns from `init` and reuses in every
+ * `compute` (lineax/_solve.py:785-790 — linear_solve skips init when a state
+ * is passed; lineax/_solver/cholesky.py:43-62 is the state).  fmode[s]
+ * (device int32) selects per system: 0 factor A and keep nothing, 1 factor A
+ * and store the factor at factors[s], 2 skip the factorisation and use the
+ * factor stored at factors[s] (A is still read by the refinement residual).
+ * `factors` is a device array of `batch` device pointers (entries of systems
+ * with fmode 0 are not read), each to n[s]² FP32 (row-major, upper triangle,
+ * lower zeroed).  A stored factor is the one a fresh factorisation makes, so
+ * results are bit-identical with and without reuse.  Other arguments and the
+ * workspace as for lxgb_posv_ragged_mixed. */
+int lxgb_posv_ragged_mixed_factors(int64_t batch, int32_t max_n, int32_t max_nrhs,
+                                   const int32_t* n, const int32_t* nrhs,
+                                   const int64_t* a_off, const double* a,
+                                   const int64_t* b_off, const double* b, double* x,
+                                   double tol, int32_t max_iter, int32_t* info,
+                                   int32_t* iters, double* berr, const int32_t* fmode,
+                                   float* const* factors, void* work, int64_t work_bytes,
+                                   void* stream);
+
 /* Tuning table of the mixed solve (no counterpart in the reference): the
  * largest order whose FP32 factor is formed in shared memory; larger systems
  * use a per-CTA slice of the workspace (through L2).  0 <= small_max <= 144,
@@ -167,6 +188,14 @@ int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
 int lxgb_posv_mixed_set_small_max(int32_t small_max);
 int32_t lxgb_posv_mixed_small_max(void);
 
+/* Second tuning switch of the mixed solve (no counterpart in the reference):
+ * on = 1 runs the trailing updates of the factor of systems above small_max
+ * (up to order 544) on the tcgen05 tensor cores (split TF32 products,
+ * FP32-level accuracy), on = 0 (default) on the CUDA cores.  Set at
+ * initialisation, like small_max.  A tensor-core completion wait that times
+ * out abandons that system with info[s] = -3 and the kernel goes on. */
+int lxgb_posv_mixed_set_tensor_cores(int32_t on);
+
 /* Allocation-free form of lxgb_posv_ragged_mixed (no counterpart in the
  * reference).  It is for callers that cannot allocate device memory when they
  * solve — an XLA/JAX FFI handler, whose device memory belongs to XLA and where
@@ -175,11 +204,16 @@ int32_t lxgb_posv_mixed_small_max(void);
  * and results are those of lxgb_posv_ragged_mixed without `work`: the scratch
  * is a fixed array of LXGB_POSV_NOALLOC_SCRATCH_BYTES (16 MiB + 256 B) inside
  * the library, which every GPU that loads the library holds until the process
- * exits.  Limits: max_n <= 1024 (larger is rejected with LXGB_INVALID_ARG);
- * systems with n > 144 factor in 16 MiB / (4·max_n²) slices, so fewer CTAs run
- * them than in the workspace form (at max_n = 512, 16 at a time); systems are
- * taken longest first when the slices leave room for the order (4 bytes per
- * system), else in index order.
+ * exits.  Limits: max_n <= 1024 (larger is rejected with LXGB_INVALID_ARG).
+ * When max_n > 144 (the largest order factored in shared memory) every CTA of
+ * the launch needs one FP32 factor slice of 4·ld² bytes (ld = max_n rounded up
+ * to a multiple of 32) in the array, so the WHOLE launch, small systems
+ * included, runs on 16 MiB / (4·ld²) CTAs instead of two per SM: 16 CTAs at
+ * max_n = 512, 4 at max_n = 1024.  Callers with mostly small systems should
+ * pass their large systems in a separate call.  With max_n <= 144 no slice is
+ * needed and the grid is the workspace form's.  Systems are taken longest
+ * first when the slices leave room for the order (4 bytes per system), else
+ * in index order.
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * Every call uses the same array and leaves its contents behind (the call
@@ -335,6 +369,94 @@ int lxgb_gmres_status(int32_t k, int64_t n, int32_t restart, int32_t parity,
                       int32_t* out, void* work, int64_t work_bytes,
                       void* stream);
 
+/* Single-call solves: the whole CG / GMRES loop on the device, the form a
+ * jax.ffi custom call needs (one call per lax.while_loop of
+ * lineax/_solver/cg.py:209 and gmres.py:215,292).  The call enqueues the
+ * start-up launches and one CUDA graph whose conditional WHILE node runs
+ * rounds of iterations until no right-hand side is active (lineax's loop
+ * condition per right-hand side) or the step budget is spent; the host never
+ * waits.  The operator (and the optional preconditioner, NULL for none) is
+ * described by value, always multiplied by `scale` (1.0 for the operator
+ * itself, -1.0 for the negated operator CG uses on negative-definite
+ * operators, lineax/_solver/cg.py:100-101):
+ *   LXGB_OP_DENSE     a: row-major n×n FP64 matrix, row stride lda
+ *                     (MatrixLinearOperator.mv, lineax/_operator.py:269);
+ *   LXGB_OP_POISSON5  the 5-point negative Laplacian on an nx×ny interior
+ *                     grid (n = nx*ny), matrix-free (a FunctionLinearOperator).
+ * b, y: k vectors of length n back to back; y holds y0 on entry when
+ * y0_given (else it is zeroed) and the solutions on return.  max_steps < 0
+ * means lineax's default 10*n with result `singular` when it is reached
+ * (cg.py:213-216); steps[c] and results[c] (device int32, RESULTS codes)
+ * are written per right-hand side.  Iterates, step counts and result codes
+ * are those of the per-iteration entry points above.  The call launches a
+ * graph of its own, so it cannot itself be captured into a stream capture.
+ * Workspaces: 256-byte aligned, no initialisation. */
+typedef enum lxgb_operator_kind {
+  LXGB_OP_DENSE = 0,
+  LXGB_OP_POISSON5 = 1,
+  LXGB_OP_SPLIT_DF = 2,  /* A = hi + lo (FP32 pair, row stride lda) applied in
+                            double-float arithmetic, as lxgb_gemv_df mode 1 */
+  LXGB_OP_LU32_INV = 3   /* M = U^{-1} L^{-1} P from lxgb_lu32_inverse (hi =
+                            L^{-1}, lo = U^{-1}, perm), as lxgb_lu32_apply
+                            mode 1: the GMRES-IR preconditioner */
+} lxgb_operator_kind;
+
+typedef struct lxgb_linear_operator {
+  int32_t kind;          /* lxgb_operator_kind */
+  int32_t reserved;      /* 0 */
+  int64_t n;             /* order */
+  const double* a;       /* LXGB_OP_DENSE */
+  int64_t lda;           /* LXGB_OP_DENSE, LXGB_OP_SPLIT_DF */
+  int64_t nx, ny;        /* LXGB_OP_POISSON5 */
+  double scale;          /* factor applied to the operator (1.0: as given) */
+  const float* hi;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV */
+  const float* lo;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV */
+  const int32_t* perm;   /* LXGB_OP_LU32_INV */
+} lxgb_linear_operator;
+
+/* CG (lineax/_solver/cg.py:114-227), stabilise_every in [0, 64] (0: never
+ * recompute the true residual; lineax's default is 10). */
+int64_t lxgb_cg_run_workspace_size(int32_t k, int64_t n, int32_t has_precond);
+int lxgb_cg_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                const lxgb_linear_operator* precond, const double* b, double* y,
+                int32_t y0_given, double rtol, double atol, int64_t max_steps,
+                int32_t stabilise_every, int32_t* steps, int32_t* results,
+                void* work, int64_t work_bytes, void* stream);
+
+/* Restarted GMRES (lineax/_solver/gmres.py:106-413), left-preconditioned,
+ * restart = min(restart, n) <= 128. */
+int64_t lxgb_gmres_run_workspace_size(int32_t k, int64_t n, int32_t restart);
+int lxgb_gmres_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                   const lxgb_linear_operator* precond, const double* b, double* y,
+                   int32_t y0_given, double rtol, double atol, int64_t max_steps,
+                   int32_t restart, int32_t stagnation_iters, int32_t* steps,
+                   int32_t* results, void* work, int64_t work_bytes, void* stream);
+
+/* GMRES-IR for the mixed-precision LU (no reference counterpart as a
+ * precision mode: lineax's GMRES, lineax/_solver/gmres.py:106-413,
+ * preconditioned by an LU, lineax/_solver/lu.py:53, refined to FP64
+ * backward error), the whole refinement loop in one call.  op: the operator
+ * as LXGB_OP_SPLIT_DF (A = hi + lo, FP64-accurate products); precond: the
+ * low-precision factor as LXGB_OP_LU32_INV.  x = 0, r = b; per outer step
+ * plain refinement x += M r until a step stalls (an inner solve that fails or
+ * a largest backward error that does not halve), from then on GMRES(restart,
+ * at most inner_max_steps restart cycles, rtol = atol = inner_rtol) on
+ * r / max|r| and x += max|r| y; then r = b - A x and the normwise backward
+ * error of each right-hand side with *anorm (device) = ||A||_inf.  Ends when
+ * every berr[c] <= tol (status[2] = 0), when a GMRES step stalls and
+ * stop_on_stall is set (status[2] = 1: the caller falls back to an FP64
+ * factorisation) or after max_outer steps (status[2] = 2); status[0] = outer
+ * steps, status[1] = 1 if
+ * the GMRES tier was reached (device int32[3]).  The loop is a while node
+ * holding an if/else node (the tier) holding the GMRES while node. */
+int64_t lxgb_gmres_ir_run_workspace_size(int32_t k, int64_t n, int32_t restart);
+int lxgb_gmres_ir_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                      const lxgb_linear_operator* precond, const double* b, double* x,
+                      const double* anorm, double tol, double inner_rtol,
+                      int32_t max_outer, int32_t restart, int32_t inner_max_steps,
+                      int32_t stagnation_iters, int32_t stop_on_stall, double* berr,
+                      int32_t* status, void* work, int64_t work_bytes, void* stream);
+
 /* Batched k-vector reductions into out[c] (device): op 0 <x_c, y_c>,
  * 1 max |x_c| (NaN propagates), 2 sum x_c².  Vector c at x + c*ldx. */
 int64_t lxgb_kreduce_workspace_size(int32_t k, int64_t n);
@@ -473,6 +595,29 @@ int64_t lxgb_geqrf_f32_tc_workspace_size(int64_t m, int64_t n);
 int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h, float* tau,
                       float* t, int32_t* err, void* work, int64_t work_bytes,
                       void* stream);
+
+/* lxgb_geqrf_f32_tc that also forms Q explicitly: the reflectors are applied
+ * to the m×m identity in the same tensor-core trailing updates, leaving q
+ * (m×m FP32 row-major, 16-byte aligned) = Q with A = Q [R; 0].  `work`:
+ * lxgb_geqrf_f32_tc_q_workspace_size(m, n) bytes.  With the triangular
+ * inverse of R (lxgb_lu32_inverse on R with identity pivots) it gives the
+ * square-system preconditioner M = R^{-1} Qᵀ of lxgb_qr32_apply: the
+ * low-precision QR factor of a mixed-precision square solve (lineax's QR
+ * solver, lineax/_solver/qr.py:55-94, recovered to FP64 accuracy by GMRES
+ * refinement; no reference counterpart as a precision mode). */
+int64_t lxgb_geqrf_f32_tc_q_workspace_size(int64_t m, int64_t n);
+int lxgb_geqrf_f32_tc_q(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                        float* t, float* q, int32_t* err, void* work, int64_t work_bytes,
+                        void* stream);
+
+/* y_r = R^{-1} (Qᵀ x_r) for nrhs FP64 vectors of length n (back to back):
+ * qt = Qᵀ (n×n FP32 row-major, full), rinv = R^{-1} (n×n FP32, upper
+ * triangle read).  mode 0 FP32, 1 double-float arithmetic.  x and y may not
+ * alias.  `work`: lxgb_qr32_apply_workspace_size(n, nrhs) bytes. */
+int64_t lxgb_qr32_apply_workspace_size(int32_t n, int32_t nrhs);
+int lxgb_qr32_apply(int32_t n, int32_t nrhs, const float* qt, const float* rinv,
+                    int32_t mode, const double* x, double* y, void* work,
+                    int64_t work_bytes, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Triangular solves.                                                        */

@@ -42,6 +42,26 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
          c_p, c_i64, c_p],
     ),
+    "lxgb_posv_ragged_mixed_factors": (
+        ctypes.c_int,
+        [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
+         c_p, c_p, c_p, c_i64, c_p],
+    ),
+    "lxgb_geqrf_f32_tc_q_workspace_size": (c_i64, [c_i64, c_i64]),
+    "lxgb_geqrf_f32_tc_q": (ctypes.c_int, [c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i64,
+                                           c_p]),
+    "lxgb_qr32_apply_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_qr32_apply": (ctypes.c_int, [c_i32, c_i32, c_p, c_p, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_cg_run_workspace_size": (c_i64, [c_i32, c_i64, c_i32]),
+    "lxgb_cg_run": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i32, c_f64, c_f64, c_i64,
+                                   c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_run_workspace_size": (c_i64, [c_i32, c_i64, c_i32]),
+    "lxgb_gmres_run": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_i32, c_f64, c_f64,
+                                      c_i64, c_i32, c_i32, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_gmres_ir_run_workspace_size": (c_i64, [c_i32, c_i64, c_i32]),
+    "lxgb_gmres_ir_run": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_f64, c_f64,
+                                         c_i32, c_i32, c_i32, c_i32, c_i32, c_p, c_p, c_p, c_i64,
+                                         c_p]),
     "lxgb_posv_ragged_mixed_noalloc": (
         ctypes.c_int,
         [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,
@@ -49,6 +69,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     ),
     "lxgb_posv_mixed_set_small_max": (ctypes.c_int, [c_i32]),
     "lxgb_posv_mixed_small_max": (c_i32, []),
+    "lxgb_posv_mixed_set_tensor_cores": (ctypes.c_int, [c_i32]),
     "lxgb_geqrf_t_elems": (c_i64, [c_i64]),
     "lxgb_geqrf_workspace_size": (c_i64, [c_i64, c_i64]),
     "lxgb_geqrf_f64": (ctypes.c_int, [c_i64, c_i64, c_p, c_i32, c_p, c_p, c_p, c_p, c_i64, c_p]),
@@ -145,6 +166,17 @@ class LxgbError(RuntimeError):
     def __init__(self, name: str, status: int, text: str):
         super().__init__(f"{name} failed with status {status}: {text}")
         self.status = status
+
+
+class LinearOperatorDesc(ctypes.Structure):
+    """struct lxgb_linear_operator (include/lxgb.h)."""
+
+    _fields_ = [("kind", c_i32), ("reserved", c_i32), ("n", c_i64), ("a", c_p),
+                ("lda", c_i64), ("nx", c_i64), ("ny", c_i64), ("scale", c_f64),
+                ("hi", c_p), ("lo", c_p), ("perm", c_p)]
+
+
+OP_DENSE, OP_POISSON5, OP_SPLIT_DF, OP_LU32_INV = 0, 1, 2, 3
 
 
 def lib_path() -> pathlib.Path:

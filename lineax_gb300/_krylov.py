@@ -11,10 +11,17 @@ Each right-hand side has device-side flags, so the host checks convergence
 only every few iterations; iterations past a right-hand side's stop leave it
 untouched, which makes every right-hand side's result the same as when it is
 solved alone.
+
+When the operator and preconditioner are dense matrices or the Poisson
+stencil (possibly negated), cg_run / gmres_run make one call of the
+single-call entry points (lxgb_cg_run / lxgb_gmres_run): the same launch
+sequence replayed by a CUDA graph's conditional while loop on the device,
+with no host round trip until the solve ends.
 """
 
 from __future__ import annotations
 
+import ctypes
 import dataclasses
 
 import torch
@@ -48,6 +55,104 @@ def block_mv(operator, x: torch.Tensor) -> torch.Tensor:
     ins = operator.in_structure()
     rows = [ravel(operator.mv(unravel(x[c], ins)), torch.float64) for c in range(x.shape[0])]
     return torch.stack(rows).contiguous()
+
+
+def device_operator(operator):
+    """(lxgb_linear_operator, tensors to keep alive) for operators the
+    single-call device loops apply themselves — dense matrices and the
+    Poisson stencil, possibly negated — or None (then the host drives the
+    loop and calls the operator every iteration)."""
+    from ._operator import NegLinearOperator, Poisson2DOperator
+
+    sign, op = 1.0, operator
+    while isinstance(op, NegLinearOperator):
+        sign, op = -sign, op.operator
+    if isinstance(op, Poisson2DOperator):
+        d = _ffi.LinearOperatorDesc(kind=_ffi.OP_POISSON5, n=op.nx * op.ny, nx=op.nx, ny=op.ny,
+                                    scale=sign * op.scale)
+        return d, ()
+    if isinstance(op, MatrixLinearOperator):
+        m = _blas.as_device_f64(op.matrix)
+        if m.ndim != 2 or m.shape[0] != m.shape[1] or m.stride(1) != 1:
+            m = m.contiguous()
+        if m.shape[0] != m.shape[1]:
+            return None
+        d = _ffi.LinearOperatorDesc(kind=_ffi.OP_DENSE, n=m.shape[0], a=m.data_ptr(),
+                                    lda=m.stride(0), scale=sign)
+        return d, (m,)
+    return None
+
+
+def _run_results(steps_d, res_d):
+    return steps_d.cpu().tolist(), res_d.cpu().tolist()
+
+
+def cg_run(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+           stabilise_every=10, preconditioner=None, y0: torch.Tensor | None = None):
+    """CG through the single-call entry point lxgb_cg_run (the loop on the
+    device), or None when the operator or preconditioner cannot be described
+    to it (the caller then runs cg_block)."""
+    od = device_operator(operator)
+    pd = device_operator(preconditioner) if preconditioner is not None else (None, ())
+    every = 0 if stabilise_every is None else int(stabilise_every)
+    if od is None or pd is None or not 0 <= every <= 64:
+        return None
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    b = b.contiguous()
+    k, n = b.shape
+    if od[0].n != n:
+        return None
+    dev = b.device
+    y = torch.empty_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone()
+    lib = _ffi.load()
+    has_pre = pd[0] is not None
+    work = _work(int(lib.lxgb_cg_run_workspace_size(k, n, int(has_pre))), dev)
+    steps_d = torch.empty(k, dtype=torch.int32, device=dev)
+    res_d = torch.empty(k, dtype=torch.int32, device=dev)
+    desc, pdesc = od[0], pd[0]
+    _ffi.call("lxgb_cg_run", k, n, ctypes.addressof(desc),
+              ctypes.addressof(pdesc) if has_pre else None, _ffi.ptr(b), _ffi.ptr(y),
+              int(y0 is not None), float(rtol), float(atol),
+              -1 if max_steps is None else int(max_steps), every, _ffi.ptr(steps_d),
+              _ffi.ptr(res_d), _ffi.ptr(work), work.numel() * 8, _stream(dev))
+    steps, results = _run_results(steps_d, res_d)
+    return KrylovResult(y, steps, results)
+
+
+def gmres_run(operator, b: torch.Tensor, *, rtol: float, atol: float, max_steps=None,
+              restart=20, stagnation_iters=20, preconditioner=None,
+              y0: torch.Tensor | None = None):
+    """GMRES through lxgb_gmres_run (the loop on the device), or None when
+    the operator or preconditioner cannot be described to it."""
+    od = device_operator(operator)
+    pd = device_operator(preconditioner) if preconditioner is not None else (None, ())
+    if od is None or pd is None:
+        return None
+    b = _blas.as_device_f64(b)
+    if b.ndim == 1:
+        b = b.reshape(1, -1)
+    b = b.contiguous()
+    k, n = b.shape
+    if od[0].n != n or min(int(restart), n) > 128:
+        return None
+    dev = b.device
+    y = torch.empty_like(b) if y0 is None else _blas.as_device_f64(y0).reshape(k, n).clone()
+    lib = _ffi.load()
+    R = min(int(restart), n)
+    work = _work(int(lib.lxgb_gmres_run_workspace_size(k, n, R)), dev)
+    steps_d = torch.empty(k, dtype=torch.int32, device=dev)
+    res_d = torch.empty(k, dtype=torch.int32, device=dev)
+    desc, pdesc = od[0], pd[0]
+    _ffi.call("lxgb_gmres_run", k, n, ctypes.addressof(desc),
+              ctypes.addressof(pdesc) if pdesc is not None else None, _ffi.ptr(b),
+              _ffi.ptr(y), int(y0 is not None), float(rtol), float(atol),
+              -1 if max_steps is None else int(max_steps), R, int(stagnation_iters),
+              _ffi.ptr(steps_d), _ffi.ptr(res_d), _ffi.ptr(work), work.numel() * 8,
+              _stream(dev))
+    steps, results = _run_results(steps_d, res_d)
+    return KrylovResult(y, steps, results)
 
 
 def _check_schedule(it: int) -> bool:

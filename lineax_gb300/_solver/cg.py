@@ -80,10 +80,10 @@ class CG(AbstractLinearSolver):
             res = _krylov.cg_poisson_mixed(operator, b, rtol=self.rtol, atol=self.atol,
                                            max_steps=self.max_steps, y0=y0b)
         else:
-            res = _krylov.cg_block(operator, b, rtol=self.rtol, atol=self.atol,
-                                   max_steps=self.max_steps,
-                                   stabilise_every=self.stabilise_every,
-                                   preconditioner=pre, y0=y0b)
+            kw = dict(rtol=self.rtol, atol=self.atol, max_steps=self.max_steps,
+                      stabilise_every=self.stabilise_every, preconditioner=pre, y0=y0b)
+            # one call with the loop on the device when the operators allow it
+            res = _krylov.cg_run(operator, b, **kw) or _krylov.cg_block(operator, b, **kw)
         x = res.y[0]
         if is_nsd:
             x = -x

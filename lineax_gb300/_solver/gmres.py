@@ -52,10 +52,11 @@ class GMRES(AbstractLinearSolver):
         b, _ = _krylov.vector_block(vector)
         y0b = None if "y0" not in options else _krylov.vector_block(y0)[0]
         pre = None if "preconditioner" not in options else preconditioner
-        res = _krylov.gmres_block(operator, b, rtol=self.rtol, atol=self.atol,
-                                  max_steps=self.max_steps, restart=self.restart,
-                                  stagnation_iters=self.stagnation_iters, preconditioner=pre,
-                                  y0=y0b)
+        kw = dict(rtol=self.rtol, atol=self.atol, max_steps=self.max_steps,
+                  restart=self.restart, stagnation_iters=self.stagnation_iters,
+                  preconditioner=pre, y0=y0b)
+        # one call with the loop on the device when the operators allow it
+        res = _krylov.gmres_run(operator, b, **kw) or _krylov.gmres_block(operator, b, **kw)
         sol = unravel(res.y[0], operator.in_structure())
         stats = {"num_steps": res.steps[0], "max_steps": self.max_steps}
         return sol, res.results[0], stats

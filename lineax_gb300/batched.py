@@ -152,10 +152,33 @@ class MixedWorkspace:
         return need <= self.nbytes
 
 
+# fmode values of lxgb_posv_ragged_mixed_factors
+FACTOR_COMPUTE, FACTOR_STORE, FACTOR_LOAD = 0, 1, 2
+
+
+class FactorPlan:
+    """Per-system factor handling of a mixed ragged solve: for each system
+    FACTOR_COMPUTE (None), FACTOR_STORE (an empty n×n FP32 device tensor that
+    receives the factor) or FACTOR_LOAD (a tensor holding a stored factor)."""
+
+    def __init__(self, modes, tensors, device):
+        ptrs = [0 if t is None else t.data_ptr() for t in tensors]
+        for m, t in zip(modes, tensors):
+            if m != FACTOR_COMPUTE and (t is None or t.dtype != torch.float32
+                                        or not t.is_contiguous()):
+                raise ValueError("stored factors are contiguous FP32 device tensors")
+        self.tensors = list(tensors)  # keeps the factors alive while the call runs
+        self.fmode = torch.tensor(list(modes), dtype=torch.int32).to(device, non_blocking=True)
+        self.fptr = torch.tensor(ptrs, dtype=torch.int64).to(device, non_blocking=True)
+
+
 def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int = 10,
                            workspace: MixedWorkspace | None = None,
-                           out: MixedResult | None = None) -> MixedResult:
-    """FP32-factor / FP64-refined solve of every SPD system of the batch."""
+                           out: MixedResult | None = None,
+                           factors: FactorPlan | None = None) -> MixedResult:
+    """FP32-factor / FP64-refined solve of every SPD system of the batch.
+    With `factors`, systems store their FP32 factor for later calls or reuse
+    a stored one instead of factoring (lxgb_posv_ragged_mixed_factors)."""
     dev = batch.a.device
     autotune.ensure_applied(dev)
     if workspace is None or not workspace.fits(batch.batch, batch.max_n, batch.max_nrhs):
@@ -167,12 +190,18 @@ def spd_solve_ragged_mixed(batch: RaggedBatch, tol: float = 1e-12, max_iter: int
             iters=torch.empty(batch.batch, dtype=torch.int32, device=dev),
             berr=torch.empty(batch.batch, dtype=torch.float64, device=dev),
         )
-    _ffi.call("lxgb_posv_ragged_mixed", batch.batch, batch.max_n, batch.max_nrhs,
+    common = (batch.batch, batch.max_n, batch.max_nrhs,
               _ffi.ptr(batch.n), _ffi.ptr(batch.nrhs), _ffi.ptr(batch.a_off),
               _ffi.ptr(batch.a), _ffi.ptr(batch.b_off), _ffi.ptr(batch.b), _ffi.ptr(out.x),
               float(tol), int(max_iter), _ffi.ptr(out.info), _ffi.ptr(out.iters),
-              _ffi.ptr(out.berr), _ffi.ptr(workspace.buf), workspace.nbytes,
-              _ffi.stream_handle(dev))
+              _ffi.ptr(out.berr))
+    if factors is None:
+        _ffi.call("lxgb_posv_ragged_mixed", *common, _ffi.ptr(workspace.buf), workspace.nbytes,
+                  _ffi.stream_handle(dev))
+    else:
+        _ffi.call("lxgb_posv_ragged_mixed_factors", *common, _ffi.ptr(factors.fmode),
+                  _ffi.ptr(factors.fptr), _ffi.ptr(workspace.buf), workspace.nbytes,
+                  _ffi.stream_handle(dev))
     return out
 
 

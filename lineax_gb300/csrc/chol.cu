@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "potrf.cuh"
+#include "tcgen05.cuh"
 #include "tri.cuh"
 
 namespace lxgb {
@@ -148,6 +149,8 @@ struct MxSmem {
   int done[kMxKc];
   int next;
   int flag;
+  unsigned tmem;                  // tensor-memory accumulator (128 columns) of the update
+  alignas(8) unsigned long long tcbar;  // completion of the update's MMAs
 };
 
 
@@ -375,8 +378,143 @@ struct MxStage {
   float brow[kMxNB][kMxStageCols];
 };
 
+// --- trailing update on the tensor cores ------------------------------------
+// C -= Wᵀ W for the upper triangle of the trailing matrix, W = U[j0:j0+nb,
+// t0:n] the block row just formed: 128×128 tiles of C, each the product of
+// two 128-row bands of Wᵀ (K = 32) held in shared memory in the 128-byte
+// swizzled K-major layout, accumulated in tensor memory by tcgen05.mma with
+// split TF32 operands (W = Wh + Wl, both rounded to TF32; Wh Whᵀ + Wh Wlᵀ +
+// Wl Whᵀ, three MMAs per K-step of 8), which keeps the update at FP32-level
+// accuracy.  Thread 0 issues the MMAs; every warp then reads its 32 TMEM
+// lanes (tile rows) × 64 columns back and subtracts them from C.
+constexpr int kTcBand = 128;
+constexpr int kTcBandFloats = kTcBand * kMxNB;  // 16 KB per band and part
+
+struct TcBands {
+  float ah[kTcBandFloats];  // band ti of Wᵀ, hi and lo parts
+  float al[kTcBandFloats];
+  float bh[kTcBandFloats];  // band tj
+  float bl[kTcBandFloats];
+};
+static_assert(sizeof(TcBands) == 4 * kTcBandFloats * 4, "band layout");
+
+// Rows [128 band, +128) of Wᵀ (Wᵀ[i][p] = U[j0+p][t0+i], zero for p >= nb or
+// i >= m) into hi/lo: row r is 128 bytes, 16-byte granule g of row r at
+// position g ^ (r & 7) — the layout smem_desc_sw128 describes.
+__device__ __forceinline__ void tc_stage_band(const float* __restrict__ U, int ldu, int j0, int nb,
+                                              int t0, int m, int band, float* hi, float* lo) {
+  // 1024 (row, granule) pairs over 256 threads: all loads first, then the
+  // splits and the shared-memory stores (the loads stay in flight together)
+  constexpr int kPer = (kTcBand * 8) / kMxThreads;
+  float v[kPer][4];
+#pragma unroll
+  for (int it = 0; it < kPer; ++it) {
+    const int e = threadIdx.x + it * kMxThreads;
+    const int r = e & (kTcBand - 1), g = e >> 7;
+    const int i = band * kTcBand + r;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int p = 4 * g + q;
+      v[it][q] = (i < m && p < nb) ? __ldg(U + (int64_t)(j0 + p) * ldu + t0 + i) : 0.0f;
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < kPer; ++it) {
+    const int e = threadIdx.x + it * kMxThreads;
+    const int r = e & (kTcBand - 1), g = e >> 7;
+    float4 h, l;
+    h.x = round_tf32(v[it][0]); l.x = round_tf32(v[it][0] - h.x);
+    h.y = round_tf32(v[it][1]); l.y = round_tf32(v[it][1] - h.y);
+    h.z = round_tf32(v[it][2]); l.z = round_tf32(v[it][2] - h.z);
+    h.w = round_tf32(v[it][3]); l.w = round_tf32(v[it][3] - h.w);
+    const int off = r * kMxNB + ((g ^ (r & 7)) << 2);
+    *reinterpret_cast<float4*>(hi + off) = h;
+    *reinterpret_cast<float4*>(lo + off) = l;
+  }
+}
+
+// Returns 0, or -3 if an MMA completion wait timed out (the factor is then
+// abandoned; a last bounded wait lets outstanding MMAs drain first).
+__device__ __noinline__ int mx_update_tc(float* U, int ldu, int j0, int nb, int t0, int m,
+                                         MxSmem& sm, TcBands& tb, unsigned& phase) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nbands = (m + kTcBand - 1) / kTcBand;
+  constexpr unsigned idesc = idesc_tf32(kTcBand, kTcBand);
+  for (int ti = 0; ti < nbands; ++ti) {
+    tc_stage_band(U, ldu, j0, nb, t0, m, ti, tb.ah, tb.al);
+    for (int tj = ti; tj < nbands; ++tj) {
+      const bool same = tj == ti;
+      if (!same) tc_stage_band(U, ldu, j0, nb, t0, m, tj, tb.bh, tb.bl);
+      // generic-proxy smem writes -> visible to the tensor core's async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const float* bh = same ? tb.ah : tb.bh;
+        const float* bl = same ? tb.al : tb.bl;
+#pragma unroll
+        for (int k = 0; k < kMxNB / 8; ++k) {  // K = 8 TF32 (32 bytes) per instruction
+          const unsigned long long adh = smem_desc_sw128(tb.ah) + ((k * 32) >> 4);
+          const unsigned long long adl = smem_desc_sw128(tb.al) + ((k * 32) >> 4);
+          const unsigned long long bdh = smem_desc_sw128(bh) + ((k * 32) >> 4);
+          const unsigned long long bdl = smem_desc_sw128(bl) + ((k * 32) >> 4);
+          mma_tf32(sm.tmem, adh, bdh, idesc, k > 0 ? 1 : 0);
+          mma_tf32(sm.tmem, adh, bdl, idesc, 1);
+          mma_tf32(sm.tmem, adl, bdh, idesc, 1);
+        }
+        mma_commit(&sm.tcbar);
+      }
+      __syncwarp();
+      const bool ok = mbar_wait(&sm.tcbar, phase & 1);
+      ++phase;
+      // one decision for the whole CTA (a wait could end differently per thread)
+      const int timed_out = __syncthreads_or(!ok);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (timed_out) {
+        if (!ok) mbar_wait(&sm.tcbar, (phase - 1) & 1);
+        __syncthreads();
+        return -3;
+      }
+      // epilogue: warp w reads TMEM lanes 32 (w % 4).. (tile rows) and the
+      // column half w / 4
+      const int r = 32 * (warp & 3) + lane;
+      const int i = ti * kTcBand + r;
+#pragma unroll 1
+      for (int cc = 0; cc < 2; ++cc) {
+        const int c0 = 64 * (warp >> 2) + 32 * cc;
+        const int jb = tj * kTcBand + c0;
+        float* dst = U + (int64_t)(t0 + min(i, m - 1)) * ldu + t0 + jb;
+        // the row's eight granules of C are loaded before anything is stored
+        float4 c[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          const int col = jb + 4 * g;
+          c[g] = (i < m && col < m && col + 3 >= i) ? *reinterpret_cast<const float4*>(dst + 4 * g)
+                                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        float v[32];
+        tmem_ld32(sm.tmem + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)c0, v);
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          const int col = jb + 4 * g;
+          if (i < m && col < m && col + 3 >= i) {
+            c[g].x -= v[4 * g + 0];
+            c[g].y -= v[4 * g + 1];
+            c[g].z -= v[4 * g + 2];
+            c[g].w -= v[4 * g + 3];
+            *reinterpret_cast<float4*>(dst + 4 * g) = c[g];
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();  // TMEM and the B band are free again
+    }
+  }
+  return 0;
+}
+
 __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
-                               MxStage& st) {
+                               MxStage& st, bool use_tc, unsigned& phase) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   mx_copy_upper(A, n, U, ldu);
   __syncthreads();
@@ -398,6 +536,21 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
     if (m <= 0) break;
     block_row_trsm<kMxNB>(U, ldu, j0, nb, t0, n, &sm.linv[0][0]);
     __syncthreads();
+    if (use_tc && m <= kMxStageCols) {
+      // tensor-core update, then the next diagonal block by warp 0
+      TcBands& tb = *reinterpret_cast<TcBands*>(
+          (reinterpret_cast<uintptr_t>(&st) + 1023) & ~static_cast<uintptr_t>(1023));
+      const int rc = mx_update_tc(U, ldu, j0, nb, t0, m, sm, tb, phase);
+      if (rc) return rc;
+      if (warp == 0) {
+        const int bad = warp_potrf_block<kMxNB>(U, ldu, t0, min(kMxNB, m), sm.rd + t0,
+                                                &sm.ublk[0][0], &sm.linv[0][0]);
+        if (lane == 0) sm.flag = bad;
+      }
+      __syncthreads();
+      if (sm.flag) return sm.flag;
+      continue;
+    }
     const bool staged = m <= kMxStageCols;
     if (staged) {
       const int m4 = (m + 3) >> 2;
@@ -887,6 +1040,11 @@ order_systems_kernel(int64_t batch, const int32_t* __restrict__ nvec, int32_t* _
   if (tid == 0) *queue = 0;
 }
 
+// Per-system factor handling of the mixed solve (fmode[s]).
+constexpr int kFactorCompute = 0;  // factor A, keep nothing
+constexpr int kFactorStore = 1;    // factor A and store the FP32 factor at fptr[s]
+constexpr int kFactorLoad = 2;     // use the factor stored at fptr[s]; A is not factored
+
 __global__ void __launch_bounds__(kMxThreads, 2)
 posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restrict__ nvec,
                   const int32_t* __restrict__ nrhs_vec, const int64_t* __restrict__ a_off,
@@ -894,10 +1052,35 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
                   const double* __restrict__ b, double* __restrict__ x, double tol, int max_iter,
                   int32_t* __restrict__ info, int32_t* __restrict__ iters,
                   double* __restrict__ berr_out, int* queue, const int32_t* __restrict__ order,
-                  float* __restrict__ factor_ws, int small_max) {
+                  float* __restrict__ factor_ws, int small_max, const int32_t* __restrict__ fmode,
+                  float* const* __restrict__ fptr, int use_tc) {
   extern __shared__ float smem_mx[];
   __shared__ MxSmem sm;
   const int tid = threadIdx.x;
+  unsigned tc_phase = 0;
+  if (use_tc) {
+    // 128 TMEM columns for the trailing-update accumulator (two CTAs per SM
+    // hold 256 of the 512)
+    if (tid == 0) {
+      mbar_init(&sm.tcbar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if ((tid >> 5) == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+                       smem_u32(&sm.tmem))
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  } else if ((tid >> 5) == 0) {
+    // A CTA of a kernel that can allocate tensor memory holds the SM's
+    // allocation permit until it gives it up; keeping it would hold the SM to
+    // one CTA of this kernel (measured: 7.5 -> 11.8 ms on the 4096-system
+    // batch), so a CTA that will not allocate gives it up at once.
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
   for (;;) {
     const int k = mx_next(queue, &sm.next);
     if (k >= batch) break;
@@ -922,16 +1105,38 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
     float* XH = vec + kMxKc * n;
     float* XL = vec + 2 * kMxKc * n;
     if (tid == 0) sm.flag = 0;
+    const int fm = fmode ? fmode[s] : kFactorCompute;
     int rc;
-    if (small) {
+    if (fm == kFactorLoad) {
+      // A factor kept from an earlier call: the upper triangle as stored, and
+      // 1/diag formed exactly as the factorisation forms it (1.0f / d).
+      const float* src = fptr[s];
+      __syncthreads();
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e - i * n;
+        if (j >= i) F[(int64_t)i * ld + j] = src[e];
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += blockDim.x) sm.rd[i] = 1.0f / F[(int64_t)i * ld + i];
+      rc = 0;
+    } else if (small) {
       mx_copy_upper(A, n, F, ld);
       __syncthreads();
       rc = mx_factor_small(F, ld, n, sm);
     } else {
       __syncthreads();
-      rc = mx_factor_large(A, F, n, ld, sm, *reinterpret_cast<MxStage*>(smem_mx));
+      rc = mx_factor_large(A, F, n, ld, sm, *reinterpret_cast<MxStage*>(smem_mx), use_tc != 0,
+                           tc_phase);
     }
     __syncthreads();
+    if (rc == 0 && fm == kFactorStore) {
+      // keep the factor for later calls (upper triangle, lower zeroed)
+      float* dst = fptr[s];
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e - i * n;
+        dst[e] = (j >= i) ? F[(int64_t)i * ld + j] : 0.0f;
+      }
+    }
     if (rc != 0) {
       for (int e = tid; e < n * nrhs; e += blockDim.x) x[b_off[s] + e] = NAN;
       if (tid == 0) { info[s] = rc; iters[s] = 0; berr_out[s] = NAN; }
@@ -955,6 +1160,13 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
     }
     if (tid == 0) { info[s] = sys_info; iters[s] = sys_iters; berr_out[s] = sys_berr; }
   }
+  if (use_tc) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if ((tid >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(sm.tmem)
+                   : "memory");
+  }
 }
 
 __global__ void reset_queue_kernel(int* queue) { *queue = 0; }
@@ -964,13 +1176,17 @@ __global__ void reset_queue_kernel(int* queue) { *queue = 0; }
 // autotune table at initialisation (lxgb_posv_mixed_set_small_max); each call
 // reads it once, and workspace sizes follow it.
 static std::atomic<int> g_mx_small_max{kMxSmallN};
+// Trailing updates of the large-system factor on the tensor cores (1) or on
+// the CUDA cores (0); a tuning switch like small_max, fixed at start-up.
+static std::atomic<int> g_mx_tc{0};
 
 static size_t mixed_smem_bytes(int max_n, int max_nrhs, int small_max) {
   (void)max_nrhs;
   const int ns = max_n < small_max ? max_n : small_max;
   const size_t small = (size_t)ns * (ns | 1) * sizeof(float) + (size_t)3 * kMxKc * ns * sizeof(float);
   size_t large = (size_t)3 * kMxKc * max_n * sizeof(float);
-  if (max_n > small_max && large < sizeof(MxStage)) large = sizeof(MxStage);
+  // the staged block row (or the tensor-core bands, aligned to 1024 bytes)
+  if (max_n > small_max && large < sizeof(MxStage) + 1024) large = sizeof(MxStage) + 1024;
   return small > large ? small : large;
 }
 
@@ -995,7 +1211,8 @@ static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs
                         const int32_t* nrhs, const int64_t* a_off, const double* a,
                         const int64_t* b_off, const double* b, double* x, double tol,
                         int32_t max_iter, int32_t* info, int32_t* iters, double* berr,
-                        void* scratch, bool ordered, int small_max, cudaStream_t st) {
+                        void* scratch, bool ordered, int small_max, cudaStream_t st,
+                        const int32_t* fmode = nullptr, float* const* fptr = nullptr) {
   char* base = reinterpret_cast<char*>(scratch);
   int* queue = reinterpret_cast<int*>(base);
   int32_t* order = ordered ? reinterpret_cast<int32_t*>(base + kQueueHeader) : nullptr;
@@ -1010,7 +1227,8 @@ static int mixed_launch(int grid, int64_t batch, int32_t max_n, int32_t max_nrhs
                 "posv_mixed: set smem");
   posv_mixed_kernel<<<(unsigned)grid, kMxThreads, smem, st>>>(
       batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x, tol, max_iter, info, iters, berr,
-      queue, order, factor_ws, small_max);
+      queue, order, factor_ws, small_max, fmode, fptr,
+      (g_mx_tc.load() && max_n > small_max) ? 1 : 0);
   return check_launch("posv_mixed");
 }
 
@@ -1073,6 +1291,12 @@ extern "C" int lxgb_posv_mixed_set_small_max(int32_t small_max) {
 
 extern "C" int32_t lxgb_posv_mixed_small_max(void) { return g_mx_small_max.load(); }
 
+extern "C" int lxgb_posv_mixed_set_tensor_cores(int32_t on) {
+  LXGB_REQUIRE(on == 0 || on == 1, "posv_mixed: tensor-core switch must be 0 or 1");
+  g_mx_tc.store(on);
+  return LXGB_SUCCESSFUL;
+}
+
 extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_nrhs,
                                       const int32_t* n, const int32_t* nrhs, const int64_t* a_off,
                                       const double* a, const int64_t* b_off, const double* b,
@@ -1095,6 +1319,31 @@ extern "C" int lxgb_posv_ragged_mixed(int64_t batch, int32_t max_n, int32_t max_
   return mixed_launch(mixed_grid(batch), batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x,
                       tol, max_iter, info, iters, berr, work, true, small_max,
                       as_stream(stream));
+}
+
+extern "C" int lxgb_posv_ragged_mixed_factors(
+    int64_t batch, int32_t max_n, int32_t max_nrhs, const int32_t* n, const int32_t* nrhs,
+    const int64_t* a_off, const double* a, const int64_t* b_off, const double* b, double* x,
+    double tol, int32_t max_iter, int32_t* info, int32_t* iters, double* berr,
+    const int32_t* fmode, float* const* factors, void* work, int64_t work_bytes, void* stream) {
+  LXGB_REQUIRE(batch >= 0 && max_n >= 0 && max_nrhs >= 0, "posv_mixed_factors: negative size");
+  if (batch == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(batch < (1LL << 31), "posv_mixed_factors: batch too large");
+  LXGB_REQUIRE(n && nrhs && a_off && a && b_off && b && x && info && iters && berr && work &&
+                   fmode && factors,
+               "posv_mixed_factors: null pointer");
+  LXGB_REQUIRE(max_iter >= 1, "posv_mixed_factors: max_iter must be >= 1");
+  LXGB_REQUIRE(max_n <= kMxMaxN, "posv_mixed_factors: max_n above 1024");
+  LXGB_REQUIRE(((uintptr_t)work & 255) == 0,
+               "posv_mixed_factors: workspace must be 256-byte aligned");
+  const int small_max = g_mx_small_max.load();
+  if (work_bytes < mixed_workspace_bytes(batch, max_n, small_max)) {
+    set_last_error("posv_mixed_factors: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  return mixed_launch(mixed_grid(batch), batch, max_n, max_nrhs, n, nrhs, a_off, a, b_off, b, x,
+                      tol, max_iter, info, iters, berr, work, true, small_max,
+                      as_stream(stream), fmode, factors);
 }
 
 // ---------------------------------------------------------------------------

@@ -521,6 +521,48 @@ extern "C" int lxgb_lu32_apply(int32_t n, int32_t nrhs, const float* linv, const
   return rc;
 }
 
+extern "C" int64_t lxgb_qr32_apply_workspace_size(int32_t n, int32_t nrhs) {
+  return 4 * vec_bytes(n, nrhs);
+}
+
+extern "C" int lxgb_qr32_apply(int32_t n, int32_t nrhs, const float* qt, const float* rinv,
+                               int32_t mode, const double* x, double* y, void* work,
+                               int64_t work_bytes, void* stream) {
+  LXGB_REQUIRE(mode == 0 || mode == 1, "qr32_apply: mode must be 0 (FP32) or 1 (double-float)");
+  LXGB_REQUIRE(n >= 0 && nrhs >= 0, "qr32_apply: negative size");
+  if (n == 0 || nrhs == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(qt && rinv && x && y && work, "qr32_apply: null pointer");
+  if (work_bytes < lxgb_qr32_apply_workspace_size(n, nrhs)) {
+    set_last_error("qr32_apply: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = as_stream(stream);
+  const int64_t vb = vec_bytes(n, nrhs);
+  char* wb = reinterpret_cast<char*>(work);
+  float* zh = reinterpret_cast<float*>(wb);
+  float* zl = reinterpret_cast<float*>(wb + vb);
+  float* th = reinterpret_cast<float*>(wb + 2 * vb);
+  float* tl = reinterpret_cast<float*>(wb + 3 * vb);
+  const int64_t total = (int64_t)n * nrhs;
+  const unsigned g = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  split_rows_kernel<<<g, 256, 0, st>>>(nrhs, n, x, n, nullptr, zh, mode ? zl : nullptr, n);
+  int rc;
+  if (mode == 0) {
+    rc = launch_gemv16<0, 0, 0>(n, n, qt, nullptr, n, nrhs, zh, nullptr, n, th, nullptr, nullptr,
+                                nullptr, n, st);
+    if (!rc)
+      rc = launch_gemv16<0, 2, 1>(n, n, rinv, nullptr, n, nrhs, th, nullptr, n, nullptr, nullptr,
+                                  y, nullptr, n, st);
+  } else {
+    rc = launch_gemv16<1, 0, 0>(n, n, qt, nullptr, n, nrhs, zh, zl, n, th, tl, nullptr, nullptr,
+                                n, st);
+    if (!rc)
+      rc = launch_gemv16<1, 2, 1>(n, n, rinv, nullptr, n, nrhs, th, tl, n, nullptr, nullptr, y,
+                                  nullptr, n, st);
+  }
+  return rc;
+}
+
 extern "C" int lxgb_split_f64(int64_t rows, int64_t cols, const double* a, int64_t lda, float* hi,
                               float* lo, int64_t ld, void* stream) {
   LXGB_REQUIRE(rows >= 0 && cols >= 0, "split_f64: negative size");

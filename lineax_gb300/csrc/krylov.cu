@@ -11,6 +11,8 @@
 // combining them in index order), so results do not depend on timing.
 #include <math.h>
 
+#include <vector>
+
 #include "common.cuh"
 #include "krylov.cuh"
 
@@ -421,13 +423,16 @@ struct GmWork {
   int R;
 };
 
+// Exactly the regions gm_carve takes, each rounded up to 256 bytes.
 static int64_t gm_ws_bytes(int k, int64_t n, int R) {
   const int P = kparts(n);
+  auto r256 = [](int64_t b) { return (b + 255) & ~(int64_t)255; };
   int64_t b = 256;
-  b += (int64_t)k * (R + 1) * n * 8;
-  b += (int64_t)k * R * (R + 1) * 8 + (int64_t)k * R * 8 + (int64_t)k * (R + 1) * 8;
-  b += (int64_t)k * 8 * 8 + (int64_t)k * 8 * 4;
-  b += (int64_t)k * P * (R + 2) * 8 + 1024;
+  b += r256((int64_t)k * (R + 1) * n * 8);
+  b += r256((int64_t)k * R * (R + 1) * 8) + r256((int64_t)k * R * 8) +
+       r256((int64_t)k * (R + 1) * 8);
+  b += r256((int64_t)k * 8 * 8) + r256((int64_t)k * 8 * 4);
+  b += r256((int64_t)k * P * (R + 2) * 8);
   return b;
 }
 
@@ -916,4 +921,750 @@ extern "C" int lxgb_gmres_status(int32_t k, int64_t n, int32_t restart, int32_t 
   GmWork w = gm_carve(work, k, n, restart);
   gm_status_kernel<<<(k + 127) / 128, 128, 0, as_stream(stream)>>>(k, w, parity & 1, out);
   return check_launch("gmres_status");
+}
+
+// ---------------------------------------------------------------------------
+// Single-call CG and GMRES: the whole loop on the device.
+//
+// lineax runs both solvers as lax.while_loops (cg.py:209, gmres.py:215,292):
+// one compiled program per solve whose loop condition is evaluated on the
+// device.  The CUDA form of that is a graph with a conditional WHILE node:
+// its body is a fixed run of iterations (the step sequences above, captured
+// from a private stream) followed by a one-thread kernel that sets the loop
+// condition from the per-right-hand-side flags — any right-hand side still
+// active — and from a round counter that bounds the number of rounds by the
+// step budget, so the loop ends even if a flag were never cleared.  The host
+// builds, launches and releases the graph; it never waits for the device.
+// ---------------------------------------------------------------------------
+namespace lxgb {
+
+__global__ void loop_cond_kernel(cudaGraphConditionalHandle h, const int* __restrict__ flags,
+                                 int k, int stride, int* __restrict__ counter, int max_rounds,
+                                 int reset) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int any = 0;
+  for (int c = 0; c < k; ++c) any |= flags[(int64_t)c * stride];
+  const int rounds = reset ? 0 : *counter + 1;
+  *counter = rounds;
+  cudaGraphSetConditional(h, (any && rounds < max_rounds) ? 1u : 0u);
+}
+
+__global__ void sub_kernel(int64_t total, const double* __restrict__ b, double* __restrict__ x) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    x[e] = b[e] - x[e];
+}
+
+__global__ void strided_copy_kernel(int64_t n, int k, const double* __restrict__ x, int64_t ldx,
+                                    double* __restrict__ y) {
+  const int c = blockIdx.y;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[(int64_t)c * n + i] = x[(int64_t)c * ldx + i];
+}
+
+// lineax's result codes from the step counts (cg.py:213-222, gmres.py:217-237).
+__global__ void cg_result_kernel(int k, CgWork w, int64_t max_steps, int max_given,
+                                 int has_scale, int32_t* __restrict__ steps,
+                                 int32_t* __restrict__ results) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  const int s = w.step[c];
+  int res = LXGB_SUCCESSFUL;
+  if (!max_given)
+    res = (s == max_steps) ? LXGB_SINGULAR : LXGB_SUCCESSFUL;
+  else if (has_scale)
+    res = (s == max_steps) ? LXGB_MAX_STEPS_REACHED : LXGB_SUCCESSFUL;
+  steps[c] = s;
+  results[c] = res;
+}
+
+__global__ void gm_result_kernel(int k, GmWork w, int64_t max_steps, int max_given,
+                                 int has_scale, int stagnation_iters,
+                                 int32_t* __restrict__ steps, int32_t* __restrict__ results) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  const int* f = w.fl + c * 8;
+  const int s = f[5];
+  int res = LXGB_SUCCESSFUL;
+  if (!max_given)
+    res = (s == max_steps) ? LXGB_SINGULAR : LXGB_SUCCESSFUL;
+  else if (has_scale)
+    res = (s == max_steps) ? LXGB_MAX_STEPS_REACHED : LXGB_SUCCESSFUL;
+  if (f[6] >= stagnation_iters) res = LXGB_STAGNATION;
+  if (f[4] && f[7]) res = LXGB_BREAKDOWN;
+  steps[c] = s;
+  results[c] = res;
+}
+
+static int64_t al256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+__global__ void scale_kernel(int64_t total, double s, double* __restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    y[e] *= s;
+}
+
+// Scratch bytes apply_op needs for k vectors of length n: room for a
+// contiguous copy of x, then the double-float products' own scratch.
+static int64_t apply_scratch_bytes(int k, int64_t n) {
+  const int64_t a = lxgb_gemv_df_workspace_size((int32_t)n, k);
+  const int64_t b = lxgb_lu32_apply_workspace_size((int32_t)n, k);
+  return al256((int64_t)k * n * 8) + al256(a > b ? a : b);
+}
+
+// y = op(x) for k vectors; x_c at x + c*ldx, y contiguous.  `tmp` holds
+// apply_scratch_bytes(k, n).
+static int apply_op(const lxgb_linear_operator& op, int k, int64_t n, const double* x,
+                    int64_t ldx, double* y, double* tmp, cudaStream_t st) {
+  if (op.kind == LXGB_OP_DENSE)
+    return lxgb_gemv_f64(n, n, op.a, op.lda, 0, k, x, ldx, y, n, op.scale, 0.0, st);
+  const int64_t vb = al256((int64_t)k * n * 8);
+  void* scratch = reinterpret_cast<char*>(tmp) + vb;
+  const int64_t sbytes = apply_scratch_bytes(k, n) - vb;
+  int rc;
+  if (op.kind == LXGB_OP_SPLIT_DF) {
+    rc = lxgb_gemv_df((int32_t)n, (int32_t)n, op.hi, op.lo, op.lda, k, x, ldx, nullptr, y, n, 1,
+                      scratch, sbytes, st);
+  } else {
+    if (ldx != n) {
+      dim3 g((unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), (unsigned)k);
+      strided_copy_kernel<<<g, 256, 0, st>>>(n, k, x, ldx, tmp);
+      x = tmp;
+    }
+    if (op.kind == LXGB_OP_POISSON5) return lxgb_poisson5_f64(op.nx, op.ny, k, op.scale, x, y, st);
+    rc = lxgb_lu32_apply((int32_t)n, k, op.hi, op.lo, op.perm, 1, x, y, scratch, sbytes, st);
+  }
+  if (!rc && op.scale != 1.0) {
+    const int64_t total = (int64_t)k * n;
+    scale_kernel<<<(unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096), 256, 0,
+                   st>>>(total, op.scale, y);
+    rc = check_launch("krylov run: scale");
+  }
+  return rc;
+}
+
+static int check_op(const lxgb_linear_operator* op, int64_t n, const char* who) {
+  if (!op) return invalid("krylov run: null operator");
+  if (op->kind == LXGB_OP_DENSE) {
+    if (!op->a || op->lda < n) {
+      set_last_error("%s: dense operator needs a matrix with lda >= n", who);
+      return LXGB_INVALID_ARG;
+    }
+    return LXGB_SUCCESSFUL;
+  }
+  if (op->kind == LXGB_OP_POISSON5) {
+    if (op->nx < 1 || op->ny < 1 || op->nx * op->ny != n) {
+      set_last_error("%s: stencil grid does not match n", who);
+      return LXGB_INVALID_ARG;
+    }
+    return LXGB_SUCCESSFUL;
+  }
+  if (op->kind == LXGB_OP_SPLIT_DF || op->kind == LXGB_OP_LU32_INV) {
+    const bool ok = op->hi && n < (1LL << 31) &&
+                    (op->kind == LXGB_OP_SPLIT_DF ? op->lda >= n : (op->lo && op->perm));
+    if (!ok) {
+      set_last_error("%s: FP32 operator needs its factor arrays (and lda >= n)", who);
+      return LXGB_INVALID_ARG;
+    }
+    return LXGB_SUCCESSFUL;
+  }
+  set_last_error("%s: unknown operator kind %d", who, op->kind);
+  return LXGB_INVALID_ARG;
+}
+
+// Graph building by stream capture.  A Capture records what is issued on its
+// root stream into a new graph.  Conditional nodes (while, if/else) are
+// appended to a stream's ongoing capture; each body is recorded from a fresh
+// private stream, so loops nest the way lax.while_loop bodies do.  Every
+// stream still capturing when the Capture is destroyed (after an error) has
+// its capture ended, so no stream is left in capture mode.
+struct Capture {
+  cudaStream_t root = nullptr;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaStream_t> open;  // streams whose capture has not ended
+  ~Capture() {
+    for (cudaStream_t s : open) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamEndCapture(s, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();  // clear an error left by an abandoned capture
+    for (cudaStream_t s : streams) cudaStreamDestroy(s);
+  }
+  int new_stream(cudaStream_t* s, const char* who) {
+    LXGB_CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking), who);
+    streams.push_back(*s);
+    return LXGB_SUCCESSFUL;
+  }
+  int begin(const char* who) {
+    int rc = new_stream(&root, who);
+    if (rc) return rc;
+    LXGB_CUDA_TRY(cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal), who);
+    open.push_back(root);
+    return LXGB_SUCCESSFUL;
+  }
+  int end(cudaStream_t s, cudaGraph_t* g, const char* who) {
+    for (size_t i = 0; i < open.size(); ++i)
+      if (open[i] == s) {
+        open.erase(open.begin() + i);
+        break;
+      }
+    LXGB_CUDA_TRY(cudaStreamEndCapture(s, g), who);
+    return LXGB_SUCCESSFUL;
+  }
+  // A handle for a conditional node that will be appended to st's capture.
+  int handle(cudaStream_t st, cudaGraphConditionalHandle* h, const char* who) {
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g = nullptr;
+    LXGB_CUDA_TRY(cudaStreamGetCaptureInfo(st, &status, nullptr, &g), who);
+    if (status != cudaStreamCaptureStatusActive || !g) {
+      set_last_error("%s: stream is not capturing", who);
+      return LXGB_CUDA_ERROR;
+    }
+    LXGB_CUDA_TRY(cudaGraphConditionalHandleCreate(h, g, 0, 0), who);
+    return LXGB_SUCCESSFUL;
+  }
+  // Appends a conditional node with `size` bodies after everything captured
+  // on st so far; bodies[i] receive fresh streams capturing into the bodies.
+  int cond(cudaStream_t st, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+           unsigned size, cudaStream_t* bodies, const char* who) {
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edata = nullptr;
+    size_t ndeps = 0;
+    LXGB_CUDA_TRY(cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, &edata, &ndeps), who);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = type;
+    cp.conditional.size = size;
+    cudaGraphNode_t node;
+    LXGB_CUDA_TRY(cudaGraphAddNode(&node, g, deps, edata, ndeps, &cp), who);
+    LXGB_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                                      cudaStreamSetCaptureDependencies),
+                  who);
+    for (unsigned i = 0; i < size; ++i) {
+      int rc = new_stream(&bodies[i], who);
+      if (rc) return rc;
+      LXGB_CUDA_TRY(cudaStreamBeginCaptureToGraph(bodies[i], cp.conditional.phGraph_out[i],
+                                                  nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal),
+                    who);
+      open.push_back(bodies[i]);
+    }
+    return LXGB_SUCCESSFUL;
+  }
+  int end_body(cudaStream_t s, const char* who) {
+    cudaGraph_t g = nullptr;
+    return end(s, &g, who);
+  }
+  // Ends the root capture, instantiates the graph and launches it on `user`
+  // (the executable graph is released once it has run).
+  int launch(cudaStream_t user, const char* who) {
+    cudaGraph_t g = nullptr;
+    int rc = end(root, &g, who);
+    if (rc) return rc;
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    LXGB_CUDA_TRY(ie, who);
+    const cudaError_t le = cudaGraphLaunch(exec, user);
+    cudaGraphExecDestroy(exec);
+    LXGB_CUDA_TRY(le, who);
+    return LXGB_SUCCESSFUL;
+  }
+};
+
+struct CgRunLayout {
+  int64_t cg, counter, r, p, matp, ay, z, tmp, total;
+};
+
+static CgRunLayout cg_run_layout(int k, int64_t n, bool pre) {
+  CgRunLayout L;
+  const int64_t v = al256((int64_t)k * n * 8);
+  L.cg = 0;
+  L.counter = al256(cg_ws_bytes(k, n));
+  L.r = L.counter + 256;
+  L.p = L.r + v;
+  L.matp = L.p + v;
+  L.ay = L.matp + v;
+  L.tmp = L.ay + v;
+  L.z = L.tmp + al256(apply_scratch_bytes(k, n));
+  L.total = L.z + (pre ? v : 0);
+  return L;
+}
+
+}  // namespace lxgb
+
+extern "C" int64_t lxgb_cg_run_workspace_size(int32_t k, int64_t n, int32_t has_precond) {
+  if (k < 1 || n < 1) return 256;
+  return cg_run_layout(k, n, has_precond != 0).total;
+}
+
+extern "C" int lxgb_cg_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                           const lxgb_linear_operator* precond, const double* b, double* y,
+                           int32_t y0_given, double rtol, double atol, int64_t max_steps,
+                           int32_t stabilise_every, int32_t* steps, int32_t* results,
+                           void* work, int64_t work_bytes, void* stream) {
+  const char* who = "cg_run";
+  LXGB_REQUIRE(k >= 1 && k <= 65535 && n >= 1, "cg_run: bad sizes");
+  LXGB_REQUIRE(b && y && steps && results && work, "cg_run: null pointer");
+  LXGB_REQUIRE(((uintptr_t)work & 255) == 0, "cg_run: workspace must be 256-byte aligned");
+  LXGB_REQUIRE(stabilise_every >= 0 && stabilise_every <= 64,
+               "cg_run: stabilise_every must be in [0, 64] (0: never)");
+  int rc = check_op(op, n, who);
+  if (rc) return rc;
+  if (precond && (rc = check_op(precond, n, who))) return rc;
+  const bool pre = precond != nullptr;
+  const CgRunLayout L = cg_run_layout(k, n, pre);
+  if (work_bytes < L.total) {
+    set_last_error("cg_run: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  char* wb = reinterpret_cast<char*>(work);
+  void* cgws = wb + L.cg;
+  const int64_t cgb = cg_ws_bytes(k, n);
+  int* counter = reinterpret_cast<int*>(wb + L.counter);
+  double* r = reinterpret_cast<double*>(wb + L.r);
+  double* p = reinterpret_cast<double*>(wb + L.p);
+  double* matp = reinterpret_cast<double*>(wb + L.matp);
+  double* ay = reinterpret_cast<double*>(wb + L.ay);
+  double* tmp = reinterpret_cast<double*>(wb + L.tmp);
+  double* z = pre ? reinterpret_cast<double*>(wb + L.z) : r;
+  const int64_t total = (int64_t)k * n;
+  const bool max_given = max_steps >= 0;
+  const int64_t max_s = max_given ? max_steps : 10 * n;
+  const int has_scale = !(atol == 0.0 && rtol == 0.0);
+  const double rcond = 2.0 * 2.220446049250313e-16 * (double)n;
+  const unsigned g = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  // iterations per round: a multiple of stabilise_every (the true-residual
+  // steps fall on fixed positions) and of 2 (the flag parity returns to 0)
+  int per = stabilise_every == 0 ? 8 : stabilise_every;
+  if (per & 1) per *= 2;
+  while (per < 8) per *= 2;
+  const int64_t rounds64 = (max_s + per - 1) / per + 1;
+  const int max_rounds = (int)(rounds64 < (1LL << 30) ? rounds64 : (1LL << 30));
+  CgWork w = cg_carve(cgws, k, n);
+  Capture cap;
+  if ((rc = cap.begin(who))) return rc;
+  cudaStream_t st = cap.root;
+  // r = b - A y0 (or b), z = M r, p = z, gamma = <z, r>, flags (cg.py:114-131)
+  if (y0_given) {
+    if ((rc = apply_op(*op, k, n, y, n, r, tmp, st))) return rc;
+    sub_kernel<<<g, 256, 0, st>>>(total, b, r);
+  } else {
+    LXGB_CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)total * 8, st), who);
+    LXGB_CUDA_TRY(cudaMemcpyAsync(r, b, (size_t)total * 8, cudaMemcpyDeviceToDevice, st), who);
+  }
+  if (pre && (rc = apply_op(*precond, k, n, r, n, z, tmp, st))) return rc;
+  if ((rc = lxgb_cg_start(k, n, r, z, p, max_s, has_scale, cgws, cgb, st))) return rc;
+  cudaGraphConditionalHandle h;
+  if ((rc = cap.handle(st, &h, who))) return rc;
+  loop_cond_kernel<<<1, 32, 0, st>>>(h, w.act, k, 1, counter, max_rounds, 1);
+  cudaStream_t sb;
+  if ((rc = cap.cond(st, h, cudaGraphCondTypeWhile, 1, &sb, who))) return rc;
+  for (int j = 0; j < per; ++j) {
+    const int par = j & 1;
+    const bool stable = stabilise_every == 1 ||
+                        (stabilise_every > 1 && (j + 1) % stabilise_every == 0);
+    if ((rc = apply_op(*op, k, n, p, n, matp, tmp, sb))) return rc;
+    if ((rc = lxgb_cg_step_alpha(k, n, matp, p, y, r, stable ? 0 : 1, par, rtol, atol, rcond,
+                                 cgws, cgb, sb)))
+      return rc;
+    if (stable) {
+      if ((rc = apply_op(*op, k, n, y, n, ay, tmp, sb))) return rc;
+      if ((rc = lxgb_cg_true_residual(k, n, b, ay, r, par, cgws, cgb, sb))) return rc;
+    }
+    if (pre && (rc = apply_op(*precond, k, n, r, n, z, tmp, sb))) return rc;
+    if ((rc = lxgb_cg_step_beta(k, n, b, r, z, p, par, max_s, has_scale, rtol, atol, cgws, cgb,
+                                sb)))
+      return rc;
+  }
+  loop_cond_kernel<<<1, 32, 0, sb>>>(h, w.act, k, 1, counter, max_rounds, 0);
+  if ((rc = cap.end_body(sb, who))) return rc;
+  cg_result_kernel<<<(k + 127) / 128, 128, 0, st>>>(k, w, max_s, max_given, has_scale, steps,
+                                                     results);
+  if ((rc = check_launch(who))) return rc;
+  return cap.launch(as_stream(stream), who);
+}
+
+namespace lxgb {
+
+struct GmRunLayout {
+  int64_t gm, counter, on, r, diff, w, t, tmp, tmp2, total;
+};
+
+static GmRunLayout gm_run_layout(int k, int64_t n, int R) {
+  GmRunLayout L;
+  const int64_t v = al256((int64_t)k * n * 8);
+  L.gm = 0;
+  L.counter = al256(gm_ws_bytes(k, n, R));
+  L.on = L.counter + 256;
+  L.r = L.on + al256((int64_t)k * 4);
+  L.diff = L.r + v;
+  L.w = L.diff + v;
+  L.t = L.w + v;
+  L.tmp = L.t + v;
+  L.tmp2 = L.tmp + v;
+  L.total = L.tmp2 + al256(apply_scratch_bytes(k, n));
+  return L;
+}
+
+// One restarted GMRES solve (lineax/_solver/gmres.py:106-413) enqueued on st,
+// which must be capturing: the dummy first pass, then a while node whose body
+// runs two outer iterations (flag parities 1 and 0) and re-evaluates the loop
+// condition, then the result codes.  y is the start vector (zero it first for
+// y0 = 0).
+struct GmresCall {
+  int k;
+  int64_t n;
+  int R;
+  const lxgb_linear_operator* op;
+  const lxgb_linear_operator* pre;
+  const double* b;
+  double* y;
+  double rtol, atol;
+  int64_t max_s;
+  int max_given;
+  int stagnation_iters;
+  void* work;  // GmRunLayout
+  int32_t* steps;
+  int32_t* results;
+};
+
+static int gmres_enqueue(Capture& cap, cudaStream_t st, const GmresCall& c, const char* who) {
+  const int k = c.k, R = c.R;
+  const int64_t n = c.n;
+  const GmRunLayout L = gm_run_layout(k, n, R);
+  char* wb = reinterpret_cast<char*>(c.work);
+  void* gmws = wb + L.gm;
+  const int64_t gmb = gm_ws_bytes(k, n, R);
+  int* counter = reinterpret_cast<int*>(wb + L.counter);
+  int32_t* on = reinterpret_cast<int32_t*>(wb + L.on);
+  double* r = reinterpret_cast<double*>(wb + L.r);
+  double* diff = reinterpret_cast<double*>(wb + L.diff);
+  double* wv = reinterpret_cast<double*>(wb + L.w);
+  double* t = reinterpret_cast<double*>(wb + L.t);
+  double* tmp = reinterpret_cast<double*>(wb + L.tmp);
+  double* tmp2 = reinterpret_cast<double*>(wb + L.tmp2);
+  const int64_t total = (int64_t)k * n;
+  const int has_scale = !(c.atol == 0.0 && c.rtol == 0.0);
+  const unsigned g = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  GmWork w = gm_carve(gmws, k, n, R);
+  // t = M (b - A y)
+  auto residual = [&](cudaStream_t s) -> int {
+    int e = apply_op(*c.op, k, n, c.y, n, tmp, tmp2, s);
+    if (e) return e;
+    sub_kernel<<<g, 256, 0, s>>>(total, c.b, tmp);
+    if (c.pre) return apply_op(*c.pre, k, n, tmp, n, t, tmp2, s);
+    LXGB_CUDA_TRY(cudaMemcpyAsync(t, tmp, (size_t)total * 8, cudaMemcpyDeviceToDevice, s), who);
+    return check_launch(who);
+  };
+  // one outer iteration of parity `par` (gmres.py:143-188, 240-300)
+  auto outer = [&](int par, int first, cudaStream_t s) -> int {
+    int e = 0;
+    if (!first) {
+      e = lxgb_gmres_cycle_begin(k, n, R, par, r, gmws, gmb, s);
+      for (int kk = 0; kk < R && !e; ++kk) {
+        const double* vk = w.V + (int64_t)kk * n;  // vector c at + c*(R+1)*n
+        e = apply_op(*c.op, k, n, vk, (int64_t)(R + 1) * n, c.pre ? tmp : wv, tmp2, s);
+        if (!e && c.pre) e = apply_op(*c.pre, k, n, tmp, n, wv, tmp2, s);
+        if (!e) e = lxgb_gmres_arnoldi(k, n, R, par, kk, wv, on, gmws, gmb, s);
+      }
+    }
+    if (!e) e = lxgb_gmres_cycle_end(k, n, R, par, first, c.y, diff, gmws, gmb, s);
+    if (!e) e = residual(s);
+    if (!e)
+      e = lxgb_gmres_outer(k, n, R, par, first, c.b, t, r, diff, c.y, c.rtol, c.atol, c.max_s,
+                           c.stagnation_iters, has_scale, gmws, gmb, s);
+    return e;
+  };
+  // start (gmres.py:192-205): r = 0, the dummy first pass
+  LXGB_CUDA_TRY(cudaMemsetAsync(r, 0, (size_t)total * 8, st), who);
+  int rc = lxgb_gmres_init(k, n, R, gmws, gmb, st);
+  if (!rc) rc = outer(0, 1, st);
+  if (rc) return rc;
+  // rounds of two outer iterations (parities 1, 0); the flags of parity 1
+  // are the loop condition after each round
+  const int64_t rounds64 = (c.max_s + 1) / 2 + 2;
+  const int max_rounds = (int)(rounds64 < (1LL << 30) ? rounds64 : (1LL << 30));
+  cudaGraphConditionalHandle h;
+  if ((rc = cap.handle(st, &h, who))) return rc;
+  loop_cond_kernel<<<1, 32, 0, st>>>(h, w.fl + 1, k, 8, counter, max_rounds, 1);
+  cudaStream_t sb;
+  if ((rc = cap.cond(st, h, cudaGraphCondTypeWhile, 1, &sb, who))) return rc;
+  rc = outer(1, 0, sb);
+  if (!rc) rc = outer(0, 0, sb);
+  if (rc) return rc;
+  loop_cond_kernel<<<1, 32, 0, sb>>>(h, w.fl + 1, k, 8, counter, max_rounds, 0);
+  if ((rc = cap.end_body(sb, who))) return rc;
+  gm_result_kernel<<<(k + 127) / 128, 128, 0, st>>>(k, w, c.max_s, c.max_given, has_scale,
+                                                     c.stagnation_iters, c.steps, c.results);
+  return check_launch(who);
+}
+
+static int gmres_prepare(int R, const char* who) {
+  // the least-squares kernel's shared memory is raised outside any capture
+  const size_t smem = (size_t)(R + 1) * (R + 2) * sizeof(double);
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gm_lstsq_kernel), (int)smem),
+                who);
+  return LXGB_SUCCESSFUL;
+}
+
+}  // namespace lxgb
+
+extern "C" int64_t lxgb_gmres_run_workspace_size(int32_t k, int64_t n, int32_t restart) {
+  if (k < 1 || n < 1 || restart < 1) return 256;
+  const int R = (int)(restart < n ? restart : n);
+  return gm_run_layout(k, n, R).total;
+}
+
+extern "C" int lxgb_gmres_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                              const lxgb_linear_operator* precond, const double* b, double* y,
+                              int32_t y0_given, double rtol, double atol, int64_t max_steps,
+                              int32_t restart, int32_t stagnation_iters, int32_t* steps,
+                              int32_t* results, void* work, int64_t work_bytes, void* stream) {
+  const char* who = "gmres_run";
+  LXGB_REQUIRE(k >= 1 && k <= 65535 && n >= 1, "gmres_run: bad sizes");
+  LXGB_REQUIRE(b && y && steps && results && work, "gmres_run: null pointer");
+  LXGB_REQUIRE(((uintptr_t)work & 255) == 0, "gmres_run: workspace must be 256-byte aligned");
+  const int R = (int)(restart < n ? restart : n);  // lineax: restart = min(restart, size)
+  LXGB_REQUIRE(R >= 1 && R <= kGmMaxRestart, "gmres_run: restart must be in [1, 128]");
+  int rc = check_op(op, n, who);
+  if (rc) return rc;
+  if (precond && (rc = check_op(precond, n, who))) return rc;
+  if (work_bytes < gm_run_layout(k, n, R).total) {
+    set_last_error("gmres_run: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  if ((rc = gmres_prepare(R, who))) return rc;
+  const bool max_given = max_steps >= 0;
+  GmresCall c{k, n, R, op, precond, b, y, rtol, atol, max_given ? max_steps : 10 * n,
+              max_given ? 1 : 0, stagnation_iters, work, steps, results};
+  Capture cap;
+  if ((rc = cap.begin(who))) return rc;
+  if (!y0_given) LXGB_CUDA_TRY(cudaMemsetAsync(y, 0, (size_t)k * n * 8, cap.root), who);
+  if ((rc = gmres_enqueue(cap, cap.root, c, who))) return rc;
+  return cap.launch(as_stream(stream), who);
+}
+
+// ---------------------------------------------------------------------------
+// Single-call GMRES-IR: the refinement loop of the mixed-precision LU solve
+// (FP32 factor, FP64-accurate residuals) on the device, around the GMRES
+// solve above.  Per outer step: in the first tier plain refinement
+// x += M r; from the first step that stalls on, GMRES on the scaled residual
+// (r / max|r|), preconditioned by M, x += max|r| y.  Then r = b - A x and the
+// normwise backward error of every right-hand side; the loop ends when all
+// are <= tol, when refinement stalls in the GMRES tier, or after max_outer
+// steps.  The tier choice is an if/else node, the GMRES loop a while node
+// inside it, both inside the outer while node.
+// ---------------------------------------------------------------------------
+namespace lxgb {
+
+struct IrState {
+  int tier, done, stop, it, inner_ok, code;
+  double prev;
+};
+
+__global__ void ir_init_kernel(IrState* s, double* ones, int k, cudaGraphConditionalHandle hl,
+                               int max_outer) {
+  for (int c = threadIdx.x; c < k; c += blockDim.x) ones[c] = 1.0;
+  if (threadIdx.x == 0) {
+    s->tier = 0;
+    s->done = s->stop = s->it = 0;
+    s->inner_ok = 1;
+    s->code = 2;
+    s->prev = INFINITY;
+    cudaGraphSetConditional(hl, max_outer > 0 ? 1u : 0u);
+  }
+}
+
+// The tier node's condition: 1 (GMRES) once refinement has stalled, else 0.
+__global__ void set_tier_handle_kernel(const IrState* s, cudaGraphConditionalHandle ht) {
+  if (threadIdx.x == 0) cudaGraphSetConditional(ht, s->tier ? 1u : 0u);
+}
+
+__global__ void ir_inner_ok_kernel(IrState* s, const int32_t* __restrict__ results, int k) {
+  if (threadIdx.x != 0) return;
+  int ok = 1;
+  if (results)
+    for (int c = 0; c < k; ++c) ok &= results[c] == LXGB_SUCCESSFUL;
+  s->inner_ok = ok;
+}
+
+// Backward errors, the stall test and the next tier / loop condition
+// (the host loop of gmres_ir in lineax_gb300/mixed.py).
+__global__ void ir_step_kernel(IrState* s, const double* __restrict__ rn,
+                               const double* __restrict__ xn, const double* __restrict__ bn,
+                               const double* __restrict__ anorm, double tol, int k, int max_outer,
+                               int stop_on_stall, double* __restrict__ berr,
+                               int32_t* __restrict__ status, cudaGraphConditionalHandle hl) {
+  if (threadIdx.x != 0) return;
+  const double an = *anorm;
+  int all = 1;
+  double mx = -INFINITY;
+  for (int c = 0; c < k; ++c) {
+    // separate roundings (no FMA contraction): the same value the host forms
+    const double den = __dadd_rn(__dmul_rn(an, xn[c]), bn[c]);
+    const double e = den > 0.0 ? __ddiv_rn(rn[c], den) : 0.0;
+    berr[c] = e;
+    all &= e <= tol;
+    mx = (e != e || mx != mx) ? NAN : fmax(mx, e);
+  }
+  s->it += 1;
+  if (all) {
+    s->done = 1;
+    s->code = 0;
+  } else {
+    const bool stalled = !s->inner_ok || !(mx <= s->prev / 2);
+    if (stalled) {
+      if (s->tier == 0) {
+        s->tier = 1;
+      } else if (stop_on_stall) {
+        s->stop = 1;
+        s->code = 1;
+      }
+    }
+  }
+  s->prev = mx;
+  const bool go = !s->done && !s->stop && s->it < max_outer;
+  if (!s->done && !s->stop && !go) s->code = 2;
+  status[0] = s->it;
+  status[1] = s->tier;
+  status[2] = s->code;
+  cudaGraphSetConditional(hl, go ? 1u : 0u);
+}
+
+struct IrRunLayout {
+  GmRunLayout gm;
+  int64_t gmres, rr, rhat, yin, tvec, rn, xn, bn, ones, gsteps, gres, state, kred, total;
+};
+
+static IrRunLayout ir_run_layout(int k, int64_t n, int R) {
+  IrRunLayout L;
+  const int64_t v = al256((int64_t)k * n * 8);
+  const int64_t kv = al256((int64_t)k * 8);
+  L.gm = gm_run_layout(k, n, R);
+  L.gmres = 0;
+  L.rr = al256(L.gm.total);
+  L.rhat = L.rr + v;
+  L.yin = L.rhat + v;
+  L.tvec = L.yin + v;
+  L.rn = L.tvec + v;
+  L.xn = L.rn + kv;
+  L.bn = L.xn + kv;
+  L.ones = L.bn + kv;
+  L.gsteps = L.ones + kv;
+  L.gres = L.gsteps + kv;
+  L.state = L.gres + kv;
+  L.kred = L.state + 256;
+  L.total = L.kred + al256(lxgb_kreduce_workspace_size(k, n));
+  return L;
+}
+
+}  // namespace lxgb
+
+extern "C" int64_t lxgb_gmres_ir_run_workspace_size(int32_t k, int64_t n, int32_t restart) {
+  if (k < 1 || n < 1 || restart < 1) return 256;
+  const int R = (int)(restart < n ? restart : n);
+  return ir_run_layout(k, n, R).total;
+}
+
+extern "C" int lxgb_gmres_ir_run(int32_t k, int64_t n, const lxgb_linear_operator* op,
+                                 const lxgb_linear_operator* precond, const double* b, double* x,
+                                 const double* anorm, double tol, double inner_rtol,
+                                 int32_t max_outer, int32_t restart, int32_t inner_max_steps,
+                                 int32_t stagnation_iters, int32_t stop_on_stall, double* berr,
+                                 int32_t* status, void* work, int64_t work_bytes, void* stream) {
+  const char* who = "gmres_ir_run";
+  LXGB_REQUIRE(k >= 1 && k <= 65535 && n >= 1, "gmres_ir_run: bad sizes");
+  LXGB_REQUIRE(b && x && anorm && berr && status && work, "gmres_ir_run: null pointer");
+  LXGB_REQUIRE(precond != nullptr, "gmres_ir_run: the refinement needs a preconditioner");
+  LXGB_REQUIRE(((uintptr_t)work & 255) == 0, "gmres_ir_run: workspace must be 256-byte aligned");
+  LXGB_REQUIRE(max_outer >= 0 && inner_max_steps >= 1, "gmres_ir_run: bad step limits");
+  const int R = (int)(restart < n ? restart : n);
+  LXGB_REQUIRE(R >= 1 && R <= kGmMaxRestart, "gmres_ir_run: restart must be in [1, 128]");
+  int rc = check_op(op, n, who);
+  if (!rc) rc = check_op(precond, n, who);
+  if (rc) return rc;
+  const IrRunLayout L = ir_run_layout(k, n, R);
+  if (work_bytes < L.total) {
+    set_last_error("gmres_ir_run: workspace too small");
+    return LXGB_WORKSPACE_TOO_SMALL;
+  }
+  if ((rc = gmres_prepare(R, who))) return rc;
+  char* wb = reinterpret_cast<char*>(work);
+  double* rr = reinterpret_cast<double*>(wb + L.rr);
+  double* rhat = reinterpret_cast<double*>(wb + L.rhat);
+  double* yin = reinterpret_cast<double*>(wb + L.yin);
+  double* tvec = reinterpret_cast<double*>(wb + L.tvec);
+  double* rn = reinterpret_cast<double*>(wb + L.rn);
+  double* xn = reinterpret_cast<double*>(wb + L.xn);
+  double* bn = reinterpret_cast<double*>(wb + L.bn);
+  double* ones = reinterpret_cast<double*>(wb + L.ones);
+  int32_t* gsteps = reinterpret_cast<int32_t*>(wb + L.gsteps);
+  int32_t* gres = reinterpret_cast<int32_t*>(wb + L.gres);
+  IrState* state = reinterpret_cast<IrState*>(wb + L.state);
+  void* kred = wb + L.kred;
+  const int64_t kredb = L.total - L.kred;
+  double* tmp = reinterpret_cast<double*>(wb + L.gm.tmp2);  // apply scratch (free outside GMRES)
+  const int64_t total = (int64_t)k * n;
+  Capture cap;
+  if ((rc = cap.begin(who))) return rc;
+  cudaStream_t st = cap.root;
+  LXGB_CUDA_TRY(cudaMemsetAsync(x, 0, (size_t)total * 8, st), who);
+  LXGB_CUDA_TRY(cudaMemcpyAsync(rr, b, (size_t)total * 8, cudaMemcpyDeviceToDevice, st), who);
+  if ((rc = lxgb_kreduce_f64(1, k, n, b, n, nullptr, 0, bn, kred, kredb, st))) return rc;
+  cudaGraphConditionalHandle hl;
+  if ((rc = cap.handle(st, &hl, who))) return rc;
+  ir_init_kernel<<<1, 128, 0, st>>>(state, ones, k, hl, max_outer);
+  cudaStream_t s1;
+  if ((rc = cap.cond(st, hl, cudaGraphCondTypeWhile, 1, &s1, who))) return rc;
+  // the tier node (its handle belongs to the outer loop's body graph): body
+  // 0 when the tier is GMRES, body 1 for plain refinement
+  cudaGraphConditionalHandle htier;
+  if ((rc = cap.handle(s1, &htier, who))) return rc;
+  set_tier_handle_kernel<<<1, 32, 0, s1>>>(state, htier);
+  cudaStream_t sb[2];
+  if ((rc = cap.cond(s1, htier, cudaGraphCondTypeIf, 2, sb, who))) return rc;
+  {  // GMRES on the scaled residual
+    cudaStream_t s = sb[0];
+    if ((rc = lxgb_kreduce_f64(1, k, n, rr, n, nullptr, 0, rn, kred, kredb, s))) return rc;
+    LXGB_CUDA_TRY(cudaMemcpyAsync(rhat, rr, (size_t)total * 8, cudaMemcpyDeviceToDevice, s), who);
+    if ((rc = lxgb_rows_scale_f64(k, n, rn, 1, rhat, s))) return rc;
+    LXGB_CUDA_TRY(cudaMemsetAsync(yin, 0, (size_t)total * 8, s), who);
+    GmresCall c{k, n, R, op, precond, rhat, yin, inner_rtol, inner_rtol, inner_max_steps, 1,
+                stagnation_iters, wb + L.gmres, gsteps, gres};
+    if ((rc = gmres_enqueue(cap, s, c, who))) return rc;
+    if ((rc = lxgb_rows_axpy_f64(k, n, rn, yin, x, s))) return rc;
+    ir_inner_ok_kernel<<<1, 32, 0, s>>>(state, gres, k);
+    if ((rc = cap.end_body(s, who))) return rc;
+  }
+  {  // plain refinement: x += M r
+    cudaStream_t s = sb[1];
+    if ((rc = apply_op(*precond, k, n, rr, n, tvec, tmp, s))) return rc;
+    if ((rc = lxgb_rows_axpy_f64(k, n, ones, tvec, x, s))) return rc;
+    ir_inner_ok_kernel<<<1, 32, 0, s>>>(state, nullptr, k);
+    if ((rc = cap.end_body(s, who))) return rc;
+  }
+  // r = b - A x, max|r|, max|x|, backward errors and the next step
+  if (op->kind == LXGB_OP_SPLIT_DF) {
+    const int64_t vb = al256(total * 8);
+    if ((rc = lxgb_gemv_df((int32_t)n, (int32_t)n, op->hi, op->lo, op->lda, k, x, n, b, rr, n, 1,
+                           reinterpret_cast<char*>(tmp) + vb, apply_scratch_bytes(k, n) - vb,
+                           s1)))
+      return rc;
+  } else {
+    if ((rc = apply_op(*op, k, n, x, n, rr, tmp, s1))) return rc;
+    sub_kernel<<<(unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096), 256, 0, s1>>>(
+        total, b, rr);
+  }
+  if ((rc = lxgb_kreduce_f64(1, k, n, rr, n, nullptr, 0, rn, kred, kredb, s1))) return rc;
+  if ((rc = lxgb_kreduce_f64(1, k, n, x, n, nullptr, 0, xn, kred, kredb, s1))) return rc;
+  ir_step_kernel<<<1, 32, 0, s1>>>(state, rn, xn, bn, anorm, tol, k, max_outer, stop_on_stall,
+                                   berr, status, hl);
+  if ((rc = check_launch(who))) return rc;
+  if ((rc = cap.end_body(s1, who))) return rc;
+  return cap.launch(as_stream(stream), who);
 }

@@ -855,6 +855,12 @@ __global__ void qr32_transpose_cvt_kernel(int64_t rows, int64_t cols, const doub
 
 static int64_t qr32_align(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
+// q = the m×m identity (row-major FP32), one CTA per row stride.
+__global__ void set_identity_rows_kernel(int64_t m, float* __restrict__ q) {
+  for (int64_t r = blockIdx.x; r < m; r += gridDim.x)
+    for (int64_t c = threadIdx.x; c < m; c += blockDim.x) q[r * m + c] = (r == c) ? 1.0f : 0.0f;
+}
+
 }  // namespace lxgb
 
 extern "C" int64_t lxgb_geqrf_f32_tc_workspace_size(int64_t m, int64_t n) {
@@ -865,10 +871,15 @@ extern "C" int64_t lxgb_geqrf_f32_tc_workspace_size(int64_t m, int64_t n) {
   return 256 + 2 * v + wp + w2;
 }
 
-extern "C" int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h, float* tau,
-                                 float* t, int32_t* err, void* work, int64_t work_bytes,
-                                 void* stream) {
-  using namespace lxgb;
+namespace lxgb {
+
+// FP32 Householder QR with tcgen05 TF32 trailing updates.  With q != nullptr
+// the reflectors are also applied to the columns of the m×m identity held as
+// the rows of q (the same two GEMMs per panel, on m rows instead of the
+// trailing n2), so q ends as Q in row-major order (row j = Qᵀ e_j).
+static int geqrf_f32_tc_driver(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                               float* t, float* q, int32_t* err, void* work, int64_t work_bytes,
+                               const char* who, cudaStream_t st) {
   LXGB_REQUIRE(m >= 0 && n >= 0, "geqrf_f32_tc: negative size");
   LXGB_REQUIRE(n <= m, "geqrf_f32_tc: needs a tall matrix (n <= m)");
   if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
@@ -877,36 +888,30 @@ extern "C" int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h
   LXGB_REQUIRE(m < (1LL << 31) && n < (1LL << 31), "geqrf_f32_tc: too large");
   LXGB_REQUIRE((((uintptr_t)h) & 15) == 0 && (((uintptr_t)work) & 255) == 0,
                "geqrf_f32_tc: h must be 16-byte and work 256-byte aligned");
-  if (work_bytes < lxgb_geqrf_f32_tc_workspace_size(m, n)) {
-    set_last_error("geqrf_f32_tc: workspace too small");
+  LXGB_REQUIRE(q == nullptr || (((uintptr_t)q) & 15) == 0, "geqrf_f32_tc: q must be 16-byte aligned");
+  const int64_t rows_w = q ? m : n;  // rows a trailing update may cover
+  if (work_bytes < lxgb_geqrf_f32_tc_workspace_size(m, rows_w)) {
+    set_last_error("%s: workspace too small", who);
     return LXGB_WORKSPACE_TOO_SMALL;
   }
-  cudaStream_t st = as_stream(stream);
   {
     dim3 grid((unsigned)((n + 31) / 32), (unsigned)((m + 31) / 32));
     qr32_transpose_cvt_kernel<<<grid, dim3(32, 8), 0, st>>>(m, n, a, h);
   }
+  if (q) {
+    const unsigned g = (unsigned)(m < 65535 ? m : 65535);
+    set_identity_rows_kernel<<<g, 256, 0, st>>>(m, q);
+  }
   const int64_t vb = qr32_align((int64_t)kQrNB * m * 4);
-  const int64_t wpb = qr32_align((int64_t)kQr32Split * n * kQrNB * 4);
+  const int64_t wpb = qr32_align((int64_t)kQr32Split * rows_w * kQrNB * 4);
   char* wb = reinterpret_cast<char*>(work) + 256;
   float* vrows = reinterpret_cast<float*>(wb);
   float* vcols = reinterpret_cast<float*>(wb + vb);
   float* wpart = reinterpret_cast<float*>(wb + 2 * vb);
   float* w2 = reinterpret_cast<float*>(wb + 2 * vb + wpb);
   const int nn = (int)n;
-  for (int j0 = 0; j0 < nn; j0 += kQrNB) {
-    const int nb = min(kQrNB, nn - j0);
-    float* Tp = t + (int64_t)(j0 / kQrNB) * kQrNB * kQrNB;
-    if (launch_qr_panel_cluster<float>(m, j0, j0 + nb, h, tau, Tp, st) != 0) {
-      set_last_error("geqrf_f32_tc: the panel's thread-block cluster cannot be scheduled");
-      return LXGB_NOT_SUPPORTED;
-    }
-    const int n2 = nn - (j0 + nb);
-    if (n2 <= 0) continue;
-    const int64_t tot = (int64_t)kQrNB * m;
-    qr32_make_v_kernel<<<(unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096), 256, 0,
-                         st>>>(m, j0, nb, h, vrows, vcols);
-    float* c = h + (int64_t)(j0 + nb) * m;  // trailing rows of h
+  // C -= (C Vᵀ) T' V on the rows c[0..rows) (each a column being transformed)
+  auto apply = [&](float* c, int rows, int j0, int nb, const float* Tp) -> int {
     const int64_t klen = m - j0;
     const int64_t chunk = ((klen + kQr32Split - 1) / kQr32Split + 31) / 32 * 32;
     int used = 0;
@@ -914,15 +919,57 @@ extern "C" int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h
       const int64_t k0 = j0 + (int64_t)sp * chunk;
       if (k0 >= m) break;
       const int64_t kl = min(chunk, m - k0);
-      int rc = gemm_tf32_nt(n2, nb, (int)kl, c + k0, m, vrows + k0, m,
-                            wpart + (int64_t)sp * n2 * kQrNB, kQrNB, 1.0f, 0.0f, err, st);
+      int rc = gemm_tf32_nt(rows, nb, (int)kl, c + k0, m, vrows + k0, m,
+                            wpart + (int64_t)sp * rows * kQrNB, kQrNB, 1.0f, 0.0f, err, st);
       if (rc) return rc;
       ++used;
     }
-    qr32_wt_kernel<<<(unsigned)((n2 + 127) / 128), 128, 0, st>>>(n2, nb, used, wpart, Tp, w2);
-    int rc = gemm_tf32_nt(n2, (int)klen, nb, w2, kQrNB, vcols + (int64_t)j0 * kQrNB, kQrNB,
-                          c + j0, m, -1.0f, 1.0f, err, st);
-    if (rc) return rc;
+    qr32_wt_kernel<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(rows, nb, used, wpart, Tp, w2);
+    return gemm_tf32_nt(rows, (int)klen, nb, w2, kQrNB, vcols + (int64_t)j0 * kQrNB, kQrNB,
+                        c + j0, m, -1.0f, 1.0f, err, st);
+  };
+  for (int j0 = 0; j0 < nn; j0 += kQrNB) {
+    const int nb = min(kQrNB, nn - j0);
+    float* Tp = t + (int64_t)(j0 / kQrNB) * kQrNB * kQrNB;
+    if (launch_qr_panel_cluster<float>(m, j0, j0 + nb, h, tau, Tp, st) != 0) {
+      set_last_error("%s: the panel's thread-block cluster cannot be scheduled", who);
+      return LXGB_NOT_SUPPORTED;
+    }
+    const int n2 = nn - (j0 + nb);
+    if (n2 <= 0 && !q) continue;
+    const int64_t tot = (int64_t)kQrNB * m;
+    qr32_make_v_kernel<<<(unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096), 256, 0,
+                         st>>>(m, j0, nb, h, vrows, vcols);
+    if (n2 > 0) {
+      int rc = apply(h + (int64_t)(j0 + nb) * m, n2, j0, nb, Tp);  // trailing rows of h
+      if (rc) return rc;
+    }
+    if (q) {
+      int rc = apply(q, (int)m, j0, nb, Tp);
+      if (rc) return rc;
+    }
   }
-  return check_launch("geqrf_f32_tc");
+  return check_launch(who);
+}
+
+}  // namespace lxgb
+
+extern "C" int lxgb_geqrf_f32_tc(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                                 float* t, int32_t* err, void* work, int64_t work_bytes,
+                                 void* stream) {
+  return lxgb::geqrf_f32_tc_driver(m, n, a, h, tau, t, nullptr, err, work, work_bytes,
+                                   "geqrf_f32_tc", lxgb::as_stream(stream));
+}
+
+extern "C" int64_t lxgb_geqrf_f32_tc_q_workspace_size(int64_t m, int64_t n) {
+  (void)n;
+  return lxgb_geqrf_f32_tc_workspace_size(m, m);
+}
+
+extern "C" int lxgb_geqrf_f32_tc_q(int64_t m, int64_t n, const double* a, float* h, float* tau,
+                                   float* t, float* q, int32_t* err, void* work,
+                                   int64_t work_bytes, void* stream) {
+  LXGB_REQUIRE(q != nullptr, "geqrf_f32_tc_q: null q");
+  return lxgb::geqrf_f32_tc_driver(m, n, a, h, tau, t, q, err, work, work_bytes,
+                                   "geqrf_f32_tc_q", lxgb::as_stream(stream));
 }

@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace lxgb {
 
@@ -31,7 +32,6 @@ constexpr int kTcStages = 4;       // TF32: 32 KB per stage
 constexpr int kTcStagesSplit = 3;  // 3xTF32: 64 KB per stage (hi and lo tiles)
 constexpr int kTcThreads = 128;
 constexpr int kTcTileBytes = kTcM * kTcK * 4;  // 16 KB per operand tile
-constexpr unsigned kSpinLimit = 1u << 26;      // bounded mbarrier waits
 
 template <int S, bool SPLIT>
 struct TcSmem {
@@ -53,36 +53,10 @@ static_assert(sizeof(TcSmem<kTcStages, false>::a) + sizeof(TcSmem<kTcStages, fal
 static_assert(sizeof(TcSmem<kTcStagesSplit, true>::a) + sizeof(TcSmem<kTcStagesSplit, true>::b) >=
                   4 * kTcTileBytes, "C tile does not fit the 3xTF32 stage buffers");
 
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
-}
-
-// Returns true when the phase with the given parity has completed, false on
-// timeout.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  const unsigned addr = smem_u32(bar);
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
@@ -94,62 +68,11 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
-// 128 bytes, 8-row groups 1024 bytes apart (stride byte offset), descriptor
-// version 1 (bits 46-47), layout type 2 = SWIZZLE_128B (bits 61-63).
-__device__ __forceinline__ unsigned long long smem_desc_sw128(const void* p) {
-  const unsigned long long addr = (smem_u32(p) & 0x3FFFFu) >> 4;
-  const unsigned long long lbo = 1;            // unused by swizzled K-major layouts
-  const unsigned long long sbo = 1024 >> 4;
-  return addr | (lbo << 16) | (sbo << 32) | (1ull << 46) | (2ull << 61);
-}
-
-// Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
-// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
-__host__ __device__ constexpr unsigned idesc_tf32(int m, int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(n >> 3) << 17) |
-         ((unsigned)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(unsigned tmem_d, unsigned long long adesc,
-                                         unsigned long long bdesc, unsigned idesc, int accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(unsigned long long* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
                    reinterpret_cast<unsigned long long>(map)),
                "r"(x), "r"(y), "r"(smem_u32(src))
                : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
-  unsigned r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-      "%28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // SPLIT (3xTF32): A = Ah + Al and B = Bh + Bl with TF32-exact hi parts;

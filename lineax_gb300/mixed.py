@@ -271,7 +271,8 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
              restart: int = 20, stagnation_iters: int = 20, max_outer: int = 20,
              inner_max_steps: int | None = None, factor: LU32 | None = None,
              inverse: InverseLU32 | None = None, split: SplitMatrix | None = None,
-             precision: str = "3xtf32", arith: str = "df", fallback: bool = False) -> IRResult:
+             precision: str = "3xtf32", arith: str = "df", fallback: bool = False,
+             qr: "SquareQR32 | None" = None, device_loop: bool = True) -> IRResult:
     """GMRES-based iterative refinement for A X = B (B: (k, n) FP64).
 
     Each refinement step solves A d = r / ||r||_inf with GMRES (lineax
@@ -292,24 +293,42 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     does not reach inner_rtol, or a refinement step that shrinks the largest
     backward error by less than 2x) and solves with the FP64 LU instead, as
     mixed-precision solvers do when the low-precision factor is too far from
-    A (kappa(A) u_f well above 1): IRResult.fallback is then True."""
+    A (kappa(A) u_f well above 1): IRResult.fallback is then True.
+
+    With `qr` (a SquareQR32 of A) the preconditioner is M = R^{-1} Qᵀ from
+    the TF32 Householder QR instead of the LU, and the fallback is the FP64
+    Householder QR solve: lineax's QR solver (lineax/_solver/qr.py:55-94) on
+    a square operator, recovered to FP64 accuracy the same way.
+
+    device_loop (arith "auto" with the LU preconditioner) runs the whole
+    refinement loop as one call of lxgb_gmres_ir_run — the same kernels in the
+    same order, with the loop decisions taken on the device — and returns to
+    the host once, at the end."""
     a64 = as_device_f64(a)
     b64 = as_device_f64(b)
     if b64.ndim == 1:
         b64 = b64.reshape(1, -1)
     b64 = b64.contiguous()
     k, n = b64.shape
-    if factor is None:
+    if factor is None and qr is None:
         factor = lu_factor_tf32(a64, precision)
     if split is None:
         split = split_matrix(a64)
     outer_op = SplitMatrixOperator(split, "df")
+    if device_loop and arith == "auto" and qr is None:
+        if inverse is None:
+            inverse = lu_inverse(factor, precision)
+        return _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart,
+                                stagnation_iters, max_outer, inner_max_steps, fallback)
     tiers = ["ir", "df"] if arith == "auto" else [arith]
     tier = 0
     made = {"inverse": inverse}
 
     def inner(t):
         kind = tiers[t]
+        if qr is not None:
+            op = outer_op if kind in ("df", "ir") else SplitMatrixOperator(split, kind)
+            return op, QRPreconditioner(qr, "df" if kind == "ir" else kind)
         if made["inverse"] is None:
             made["inverse"] = lu_inverse(factor, precision)
         op = outer_op if kind in ("df", "ir") else SplitMatrixOperator(split, kind)
@@ -349,10 +368,47 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
             tier += 1
             inner_op, pre = inner(tier)
         elif fallback and stalled:
-            return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
+            return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps,
+                                  qr is not None)
     if fallback and not converged:
-        return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps)
+        return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps,
+                              qr is not None)
     return IRResult(x, berr, it, inner_steps, converged, inverse=made["inverse"])
+
+
+def _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart, stagnation_iters,
+                     max_outer, inner_max_steps, fallback) -> IRResult:
+    """gmres_ir's "auto" loop as one lxgb_gmres_ir_run call."""
+    import ctypes
+
+    k, n = b64.shape
+    dev = b64.device
+    op = _ffi.LinearOperatorDesc(kind=_ffi.OP_SPLIT_DF, n=n, lda=n, scale=1.0,
+                                 hi=split.hi.data_ptr(), lo=split.lo.data_ptr())
+    pre = _ffi.LinearOperatorDesc(kind=_ffi.OP_LU32_INV, n=n, scale=1.0,
+                                  hi=inverse.linv.data_ptr(), lo=inverse.uinv.data_ptr(),
+                                  perm=inverse.perm.data_ptr())
+    anorm = norm_inf(a64).reshape(1)
+    x = torch.empty_like(b64)
+    berr = torch.empty(k, dtype=torch.float64, device=dev)
+    status = torch.zeros(3, dtype=torch.int32, device=dev)
+    R = min(int(restart), n)
+    wbytes = int(_ffi.load().lxgb_gmres_ir_run_workspace_size(k, n, R))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    inner_steps = 5 if inner_max_steps is None else int(inner_max_steps)
+    _ffi.call("lxgb_gmres_ir_run", k, n, ctypes.addressof(op), ctypes.addressof(pre),
+              _ffi.ptr(b64), _ffi.ptr(x), _ffi.ptr(anorm), float(tol), float(inner_rtol),
+              int(max_outer), R, inner_steps, int(stagnation_iters), int(bool(fallback)),
+              _ffi.ptr(berr), _ffi.ptr(status), _ffi.ptr(work), work.numel() * 8,
+              _ffi.stream_handle(dev))
+    outer, reached_gmres, code = status.cpu().tolist()
+    berr_h = berr.cpu().tolist()
+    converged = code == 0
+    if fallback and not converged:
+        outer_op = SplitMatrixOperator(split, "df")
+        return _fp64_fallback(a64, b64, outer_op, float(anorm.item()), _kmax(b64).cpu(), tol,
+                              outer, [int(reached_gmres)] * outer)
+    return IRResult(x, berr_h, outer, [int(reached_gmres)] * outer, converged, inverse=inverse)
 
 
 def _berr(r, x, anorm, bnorm) -> list:
@@ -362,12 +418,17 @@ def _berr(r, x, anorm, bnorm) -> list:
             else 0.0 for c in range(r.shape[0])]
 
 
-def _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps) -> IRResult:
-    """FP64 LU solve (lxgb_getrf/getrs) after GMRES-IR stalled."""
+def _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps,
+                   use_qr: bool = False) -> IRResult:
+    """FP64 LU solve (lxgb_getrf/getrs), or with use_qr the FP64 Householder
+    QR solve (lxgb_geqrf/ormqr/trsm), after GMRES-IR stalled."""
     from . import _dense
 
-    lu, piv = _dense.lu_factor(a64)
-    x = _dense.lu_solve(lu, piv, b64)
+    if use_qr:
+        x = qr_solve_f64(_dense.geqrf(a64), b64)
+    else:
+        lu, piv = _dense.lu_factor(a64)
+        x = _dense.lu_solve(lu, piv, b64)
     berr = _berr(outer_op.residual(x, b64), x, anorm, bnorm)
     return IRResult(x, berr, it, inner_steps, all(e <= tol for e in berr), fallback=True)
 
@@ -488,3 +549,77 @@ def qr_lstsq(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, max_iter: 
             break
     return LstsqResult(x, it, steps, converged)
 
+
+
+# ---------------------------------------------------------------------------
+# Square systems through the QR factor: TF32 Householder QR with Q formed
+# explicitly, M = R^{-1} Qᵀ as the GMRES-IR preconditioner.
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class SquareQR32:
+    qt: torch.Tensor    # Qᵀ, n×n FP32
+    rinv: torch.Tensor  # R^{-1}, n×n FP32 (zeros below the diagonal)
+
+
+def qr_square_tf32(a: torch.Tensor) -> SquareQR32:
+    """A = Q R for a square A (n % 4 == 0): FP32 Householder QR with tcgen05
+    TF32 updates that also forms Q (lxgb_geqrf_f32_tc_q), and R^{-1} by the
+    tensor-core triangular inversion (3xTF32)."""
+    a64 = as_device_f64(a).contiguous()
+    n = a64.shape[0]
+    if a64.shape != (n, n) or n % 4:
+        raise ValueError("qr_square_tf32 needs a square matrix with n a multiple of 4")
+    dev = a64.device
+    lib = _ffi.load()
+    h = torch.empty((n, n), dtype=torch.float32, device=dev)
+    tau = torch.empty(n, dtype=torch.float32, device=dev)
+    t = torch.empty(max(1, int(lib.lxgb_geqrf_t_elems(n))), dtype=torch.float32, device=dev)
+    q = torch.empty((n, n), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    wbytes = int(lib.lxgb_geqrf_f32_tc_q_workspace_size(n, n))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    _ffi.call("lxgb_geqrf_f32_tc_q", n, n, _ffi.ptr(a64), _ffi.ptr(h), _ffi.ptr(tau), _ffi.ptr(t),
+              _ffi.ptr(q), _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8,
+              _ffi.stream_handle(dev))
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the QR update")
+    del work, t, tau
+    r_sq = h.t().contiguous()  # R on and above the diagonal
+    del h
+    piv = torch.arange(n, dtype=torch.int32, device=dev)
+    inv = lu_inverse(LU32(r_sq, piv, torch.zeros(1, dtype=torch.int32, device=dev)), "3xtf32")
+    return SquareQR32(q.t().contiguous(), inv.uinv)
+
+
+class QRPreconditioner(_BlockOperator):
+    """M x = R^{-1} (Qᵀ x) for a block of FP64 vectors (lxgb_qr32_apply),
+    in FP32 ("fp32") or double-float ("df") arithmetic."""
+
+    def __init__(self, qr: SquareQR32, arith: str = "df"):
+        super().__init__(qr.qt.shape[0])
+        self.qr, self.mode = qr, ARITH[arith]
+
+    def mv_block(self, x: torch.Tensor) -> torch.Tensor:
+        xb = as_device_f64(x).contiguous()
+        k, n = xb.shape
+        out = torch.empty_like(xb)
+        wbytes = int(_ffi.load().lxgb_qr32_apply_workspace_size(n, k))
+        work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=xb.device)
+        _ffi.call("lxgb_qr32_apply", n, k, _ffi.ptr(self.qr.qt), _ffi.ptr(self.qr.rinv),
+                  self.mode, _ffi.ptr(xb), _ffi.ptr(out), _ffi.ptr(work), work.numel() * 8,
+                  _ffi.stream_handle(xb.device))
+        return out
+
+
+def qr_solve_f64(factor, b: torch.Tensor) -> torch.Tensor:
+    """x_r = R^{-1} (Qᵀ b_r)[:n] with an FP64 factor from _dense.geqrf of a
+    square or tall operator (lineax/_solver/qr.py:87-92), for a (k, m) block."""
+    from . import _dense
+
+    h, tau, t = factor
+    n = h.shape[0]
+    b64 = as_device_f64(b)
+    if b64.ndim == 1:
+        b64 = b64.reshape(1, -1)
+    qhb = _dense.ormqr(h, tau, t, b64.contiguous(), trans=True)[:, :n].contiguous()
+    return _dense.trsv(h, qhb, lower=True, trans=True, unit=False)

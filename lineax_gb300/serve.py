@@ -2,41 +2,60 @@
 
 Requests are dense square systems A X = B (1 to 16 right-hand sides) tagged
 with the lineax solver the client asked for (LU, Cholesky or QR) and an
-operator id; a request may omit A and reuse an operator the server has seen,
-in which case a resident factor (kept in device memory under an LRU policy)
-skips the factorisation.  Each scheduling round admits the queued requests
-that have arrived, first come first served, while their device footprint
-plus the resident factors fits the HBM budget, and runs them grouped by
-route:
+operator id; a request may omit A and reuse an operator the server has seen.
+What a solver's `init` produces for an operator (its factor state, the
+object lineax reuses when `linear_solve` is given `state`,
+lineax/_solve.py:785-790) stays resident in device memory under an LRU
+policy, so a request on a resident operator skips the factorisation.  Each
+scheduling round admits the queued requests that have arrived, first come
+first served, while their device footprint plus the resident operators fits
+the HBM budget, and runs them grouped by route:
 
   chol_ragged  Cholesky requests with n <= 1024: one launch of the ragged
                mixed-precision SPD kernel (FP32 factor, FP64-accurate
-               refinement) for the whole group; systems it does not solve to
-               the tolerance are re-solved by FP64 LU.
-  lu_small     other requests with n <= 168: batched FP64 LU, one launch per
+               refinement) for the whole group, new operators storing their
+               FP32 factor and resident ones loading it instead of factoring
+               (lxgb_posv_ragged_mixed_factors); systems it does not solve to
+               the tolerance are re-solved by FP64 LU.  FP64 mode: the ragged
+               FP64 Cholesky for new operators, the resident FP64 factor's
+               solve for the others.
+  lu_small     LU requests with n <= 168: batched FP64 LU, one launch per
                distinct order (each system's arithmetic is the same as alone;
                right-hand-side blocks are zero padded, and each vector is
                solved independently).
-  lu_mixed     the rest: FP32 LU with TF32/3xTF32 tensor-core updates, its
-               triangular inverses, and refinement to FP64 backward error
-               (lineax_gb300.mixed: plain refinement, then GMRES-IR, then FP64
-               LU when refinement stalls); the factor stays resident for later
-               requests on the operator.
+  lu_mixed     LU requests above that, and Cholesky requests with n > 1024:
+               FP32 LU with 3xTF32 tensor-core updates, its triangular
+               inverses, refinement to FP64 backward error (lineax_gb300.mixed:
+               plain refinement, then GMRES-IR, then FP64 LU when refinement
+               stalls); factor, inverses and the split A stay resident.
+  qr_mixed     QR requests with n > 168: FP32 Householder QR with TF32
+               tensor-core updates and Q formed explicitly, R^{-1} on the
+               tensor cores, GMRES-IR preconditioned by R^{-1} Qᵀ (FP64 QR
+               when refinement stalls); Qᵀ, R^{-1} and the split A stay
+               resident.
+  qr_f64       QR requests with n <= 168 (both modes) and every QR request in
+               FP64 mode: FP64 Householder QR (lineax's QR solver), the
+               factor resident.
+  lu_f64 / chol_f64   FP64 mode above n = 168 (LU) and 1024 (Cholesky,
+               multi-CTA FP64 factor): the plain FP64 GPU path with resident
+               factors.
 
 Serving is continuous: run() keeps admitting requests as they arrive and as
 memory frees up while earlier work is still on the GPU.  Admitted work goes
 to a pool of worker threads, each with its own CUDA stream (a ragged
 Cholesky group or a small-LU group is one job, each large request is one
 job), so requests overlap on the device; a job's device memory is released
-back to the admission budget when it completes.
+back to the admission budget when it completes.  A resident operator made on
+one worker's stream carries a CUDA event recorded after its factorisation;
+a job on another stream waits on that event before it reads the operator and
+marks the operator's tensors as used by its stream (record_stream), so
+neither an unfinished factor nor freed memory is ever read.
 
 mode="fp64" serves the same requests with the plain FP64 GPU path of this
-library (ragged FP64 Cholesky, FP64 LU) on one stream: the denominator of
-the mixed path's speed-up.  A square QR request is served by LU in both modes: for a
-nonsingular square A both define the same solution, and lineax's own
-AutoLinearSolver picks LU for square operators (lineax/_solve.py:555-600).
-Every completion carries its normwise backward error; a request's result
-does not depend on what else was in its batch.
+library on one stream: the denominator of the mixed path's speed-up.  Every
+completion carries its normwise backward error; a request's result does not
+depend on what else was in its batch or on whether its operator was
+resident.
 """
 
 from __future__ import annotations
@@ -80,7 +99,7 @@ class Completion:
     x: torch.Tensor       # (nrhs, n) FP64 on the device
     berr: float           # max normwise backward error over the right-hand sides
     route: str
-    fallback: bool        # re-solved by FP64 LU
+    fallback: bool        # re-solved by the FP64 path after refinement stalled
     reused: bool          # served from a resident factor
     finished: float = 0.0
     latency: float = 0.0
@@ -89,8 +108,12 @@ class Completion:
 def route_of(kind: str, n: int, mode: str) -> str:
     if kind not in KINDS:
         raise ValueError(f"unknown request kind {kind!r}")
-    if kind == "cholesky" and n <= RAGGED_CHOL_MAX:
-        return "chol_ragged"
+    if kind == "cholesky":
+        if n <= RAGGED_CHOL_MAX:
+            return "chol_ragged"
+        return "lu_mixed" if mode == "mixed" else "chol_f64"
+    if kind == "qr":
+        return "qr_mixed" if (mode == "mixed" and n > SMALL_LU_MAX) else "qr_f64"
     if n <= SMALL_LU_MAX:
         return "lu_small"
     return "lu_mixed" if mode == "mixed" else "lu_f64"
@@ -99,24 +122,31 @@ def route_of(kind: str, n: int, mode: str) -> str:
 def footprint(route: str, n: int, nrhs: int) -> int:
     """Device bytes a request holds while it is being served."""
     vec = 8 * 8 * n * max(nrhs, 1)  # b, x, residual and workspace vectors
+    n4 = (n + 3) // 4 * 4
     if route == "chol_ragged":
-        return 8 * n * n + 4 * n * n + vec
+        return resident_bytes(route, n) + 4 * n * n + vec   # + the packed copy of A
     if route == "lu_small":
         return 3 * 8 * SMALL_LU_MAX * SMALL_LU_MAX + vec
-    if route == "lu_f64":
-        return 2 * 8 * n * n + vec
-    n4 = (n + 3) // 4 * 4
+    if route in ("lu_f64", "chol_f64", "qr_f64"):
+        return resident_bytes(route, n) + vec
+    if route == "qr_mixed":
+        return resident_bytes(route, n) + 20 * n4 * n4 + vec  # h, q, R, inversion work
     return resident_bytes(route, n) + 5 * 4 * 64 * n4 + vec
 
 
 def resident_bytes(route: str, n: int) -> int:
     """Bytes of what stays resident for an operator between requests."""
+    n4 = (n + 3) // 4 * 4
     if route == "lu_mixed":
-        n4 = (n + 3) // 4 * 4
         # A (FP64), FP32 factor, both triangular inverses, A as a hi + lo pair
         return 8 * n4 * n4 + 4 * n4 * n4 + 8 * n4 * n4 + 8 * n4 * n4
-    if route == "lu_f64":
-        return 2 * 8 * n * n  # A and its FP64 factor
+    if route == "qr_mixed":
+        # A (FP64), A as a hi + lo pair, Qᵀ and R^{-1} (FP32)
+        return 8 * n4 * n4 + 8 * n4 * n4 + 4 * n4 * n4 + 4 * n4 * n4
+    if route == "chol_ragged":
+        return 8 * n * n + 8 * n * n  # A and its factor (FP32 mixed, FP64 plain: the larger)
+    if route in ("lu_f64", "chol_f64", "qr_f64"):
+        return 2 * 8 * n * n + 8 * 32 * n  # A and its FP64 factor (+ QR's T blocks)
     return 8 * n * n          # the operator itself
 
 
@@ -221,21 +251,34 @@ def _berr(a: torch.Tensor, x: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return r.abs().amax(dim=1) / (anorm * x.abs().amax(dim=1) + b.abs().amax(dim=1))
 
 
-@dataclasses.dataclass
-class _MixedOperator:
-    n: int
-    n4: int
-    a: torch.Tensor
-    factor: mixed.LU32
-    inverse: mixed.InverseLU32
-    split: mixed.SplitMatrix
+class _Resident:
+    """What stays on the device for an operator: `a` (the FP64 operator,
+    padded where the route pads) and the route's factor tensors.  `ready`
+    is a CUDA event recorded on the creating stream after the factorisation
+    was issued."""
 
+    def __init__(self, a: torch.Tensor, **parts):
+        self.a = a
+        self.parts = parts
+        self.ready = None
 
-@dataclasses.dataclass
-class _F64Operator:
-    a: torch.Tensor
-    lu: torch.Tensor
-    piv: torch.Tensor
+    def __getattr__(self, name):
+        parts = self.__dict__.get("parts", {})
+        if name in parts:
+            return parts[name]
+        raise AttributeError(name)
+
+    def tensors(self):
+        out = [self.a]
+        for v in self.parts.values():
+            if isinstance(v, torch.Tensor):
+                out.append(v)
+            elif dataclasses.is_dataclass(v):
+                out += [getattr(v, f.name) for f in dataclasses.fields(v)
+                        if isinstance(getattr(v, f.name), torch.Tensor)]
+            elif isinstance(v, tuple):
+                out += [t for t in v if isinstance(t, torch.Tensor)]
+        return out
 
 
 class SolveServer:
@@ -259,6 +302,29 @@ class SolveServer:
     def register(self, op_id, a_host: torch.Tensor) -> None:
         self.registry[op_id] = a_host
 
+    # -- resident operators ----------------------------------------------------
+
+    def _acquire(self, op_id):
+        """The resident operator op_id, made safe to read on this thread's
+        stream (waits for its factorisation, pins its memory), or None."""
+        res = self.sched.lookup(op_id)
+        if res is None:
+            return None
+        st = torch.cuda.current_stream(self.device)
+        if res.ready is not None:
+            st.wait_event(res.ready)
+        for t in res.tensors():
+            t.record_stream(st)
+        return res
+
+    def _publish(self, op_id, route: str, n: int, res: _Resident) -> None:
+        """Make a new resident operator visible to other streams: record the
+        event that orders its factorisation before any later reader."""
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        res.ready = ev
+        self.sched.remember(op_id, resident_bytes(route, n), res)
+
     # -- execution ------------------------------------------------------------
 
     def _matrix(self, req: Request) -> torch.Tensor:
@@ -276,40 +342,81 @@ class SolveServer:
         return _dense.lu_solve(lu, piv, b), lu, piv
 
     def _run_chol(self, reqs: list) -> list:
-        mats = [self._matrix(r) for r in reqs]
+        if self.mode == "fp64":
+            return self._run_chol_f64(reqs)
+        found = [self._acquire(r.op_id) for r in reqs]
+        mats = [res.a if res is not None else self._matrix(r) for r, res in zip(reqs, found)]
         rhs = [self._rhs(r) for r in reqs]
         rb = batched.RaggedBatch.from_lists(mats, rhs, device=self.device)
+        modes, ftens = [], []
+        for res, r in zip(found, reqs):
+            if res is not None:
+                modes.append(batched.FACTOR_LOAD)
+                ftens.append(res.factor)
+            else:
+                modes.append(batched.FACTOR_STORE)
+                ftens.append(torch.empty((r.n, r.n), dtype=torch.float32, device=self.device))
+        plan = batched.FactorPlan(modes, ftens, self.device)
+        ws = getattr(self._tls, "ws", None)
+        if ws is None or not ws.fits(rb.batch, rb.max_n, rb.max_nrhs):
+            ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, self.device)
+            self._tls.ws = ws
+        res_k = batched.spd_solve_ragged_mixed(rb, tol=self.tol, workspace=ws, factors=plan)
+        info = res_k.info.cpu().tolist()
+        berr = res_k.berr.cpu().tolist()
         out = []
-        if self.mode == "mixed":
-            ws = getattr(self._tls, "ws", None)
-            if ws is None or not ws.fits(rb.batch, rb.max_n, rb.max_nrhs):
-                ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, self.device)
-                self._tls.ws = ws
-            res = batched.spd_solve_ragged_mixed(rb, tol=self.tol, workspace=ws)
-            info = res.info.cpu().tolist()
-            berr = res.berr.cpu().tolist()
-            for s, req in enumerate(reqs):
-                x = rb.system_b(res.x, s).clone()
-                if info[s] != 0 or not berr[s] <= self.tol:
-                    x, _, _ = self._fp64_lu(mats[s], rhs[s])
-                    e = float(_berr(mats[s], x, rhs[s]).max())
-                    out.append(Completion(req.rid, x, e, "chol_ragged", True, False))
-                else:
-                    out.append(Completion(req.rid, x, berr[s], "chol_ragged", False, False))
-            return out
-        x, info = batched.cholesky_solve_ragged(rb)
-        info = info.cpu().tolist()
-        errs = []
-        xs = []
+        for s, req in enumerate(reqs):
+            x = rb.system_b(res_k.x, s).clone()
+            reused = found[s] is not None
+            if info[s] != 0 or not berr[s] <= self.tol:
+                x, _, _ = self._fp64_lu(mats[s], rhs[s])
+                e = float(_berr(mats[s], x, rhs[s]).max())
+                out.append(Completion(req.rid, x, e, "chol_ragged", True, reused))
+                continue
+            if not reused:
+                self._publish(req.op_id, "chol_ragged", req.n,
+                              _Resident(mats[s], factor=ftens[s]))
+            out.append(Completion(req.rid, x, berr[s], "chol_ragged", False, reused))
+        return out
+
+    def _run_chol_f64(self, reqs: list) -> list:
+        """Plain FP64: one ragged potrf launch for the new operators, then one
+        ragged potrs launch for every request, resident operators with their
+        stored FP64 factor (the same solve kernel either way)."""
+        found = [self._acquire(r.op_id) for r in reqs]
+        rhs = [self._rhs(r) for r in reqs]
+        mats = [res.a if res is not None else self._matrix(r) for r, res in zip(reqs, found)]
+        us = [res.u if res is not None else None for res in found]
+        fallback = [False] * len(reqs)
+        fresh = [s for s, res in enumerate(found) if res is None]
+        if fresh:
+            rbf = batched.RaggedBatch.from_lists([mats[s] for s in fresh],
+                                                 [rhs[s] for s in fresh], device=self.device)
+            u, info = batched.cholesky_factor_ragged(rbf)
+            info = info.cpu().tolist()
+            for j, s in enumerate(fresh):
+                n, off = reqs[s].n, rbf.a_off_host[j]
+                us[s] = u[off: off + n * n].view(n, n).clone()
+                fallback[s] = info[j] != 0
+        ok = [s for s in range(len(reqs)) if not fallback[s]]
+        xs = [None] * len(reqs)
+        if ok:
+            rb = batched.RaggedBatch.from_lists([mats[s] for s in ok], [rhs[s] for s in ok],
+                                                device=self.device)
+            x, _ = batched.cholesky_solve_ragged(
+                rb, torch.cat([us[s].reshape(-1) for s in ok]))
+            for j, s in enumerate(ok):
+                xs[s] = rb.system_b(x, j).clone()
+                if found[s] is None:
+                    self._publish(reqs[s].op_id, "chol_ragged", reqs[s].n,
+                                  _Resident(mats[s], u=us[s]))
         for s in range(len(reqs)):
-            xv = rb.system_b(x, s).clone()
-            if info[s] != 0:
-                xv, _, _ = self._fp64_lu(mats[s], rhs[s])
-            xs.append(xv)
-            errs.append(_berr(mats[s], xv, rhs[s]).max())
-        errs = torch.stack(errs).cpu().tolist() if errs else []
-        return [Completion(r.rid, xs[s], errs[s], "chol_ragged", info[s] != 0, False)
-                for s, r in enumerate(reqs)]
+            if fallback[s]:
+                xs[s], _, _ = self._fp64_lu(mats[s], rhs[s])
+        errs = torch.stack([_berr(mats[s], xs[s], rhs[s]).max() for s in range(len(reqs))])
+        errs = errs.cpu().tolist()
+        return [Completion(r.rid, xs[s], errs[s], "chol_ragged", fallback[s],
+                           found[s] is not None) for s, r in enumerate(reqs)]
 
     def _run_small(self, reqs: list) -> list:
         mats = [self._matrix(r) for r in reqs]
@@ -333,58 +440,72 @@ class SolveServer:
         return [Completion(r.rid, xs[s], errs[s], "lu_small", False, False)
                 for s, r in enumerate(reqs)]
 
+    def _padded_rhs(self, req: Request, n4: int) -> torch.Tensor:
+        b = self._rhs(req)
+        if n4 == req.n:
+            return b
+        return torch.cat([b, torch.zeros((req.nrhs, n4 - req.n), dtype=torch.float64,
+                                         device=b.device)], 1)
+
     def _run_mixed(self, req: Request) -> Completion:
-        op = self.sched.lookup(req.op_id)
-        reused = op is not None
-        if op is None:
-            a = self._matrix(req)
-            n4 = (req.n + 3) // 4 * 4
-            ap = _pad_identity(a, n4)
+        res = self._acquire(req.op_id)
+        reused = res is not None
+        n4 = (req.n + 3) // 4 * 4
+        if res is None:
+            ap = _pad_identity(self._matrix(req), n4)
             f = mixed.lu_factor_tf32(ap, self.precision)
-            op = _MixedOperator(req.n, n4, ap, f, mixed.lu_inverse(f, self.precision),
-                                mixed.split_matrix(ap))
-        b = self._rhs(req)
-        bp = b if op.n4 == req.n else torch.cat(
-            [b, torch.zeros((req.nrhs, op.n4 - req.n), dtype=torch.float64, device=b.device)], 1)
-        res = mixed.gmres_ir(op.a, bp, tol=self.tol, max_outer=20, inner_max_steps=5, restart=8,
-                             factor=op.factor, inverse=op.inverse, split=op.split,
-                             precision=self.precision, arith="auto", fallback=True)
-        self.sched.remember(req.op_id, resident_bytes("lu_mixed", req.n), op)
-        x = res.x[:, : req.n].contiguous()
-        return Completion(req.rid, x, max(res.berr), "lu_mixed", res.fallback, reused)
+            res = _Resident(ap, factor=f, inverse=mixed.lu_inverse(f, self.precision),
+                            split=mixed.split_matrix(ap))
+            self._publish(req.op_id, "lu_mixed", req.n, res)
+        ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
+                            inner_max_steps=5, restart=8, factor=res.factor,
+                            inverse=res.inverse, split=res.split, precision=self.precision,
+                            arith="auto", fallback=True)
+        x = ir.x[:, : req.n].contiguous()
+        return Completion(req.rid, x, max(ir.berr), "lu_mixed", ir.fallback, reused)
 
-    def _run_f64(self, req: Request) -> Completion:
-        op = self.sched.lookup(req.op_id)
-        reused = op is not None
-        if op is None:
+    def _run_qr_mixed(self, req: Request) -> Completion:
+        res = self._acquire(req.op_id)
+        reused = res is not None
+        n4 = (req.n + 3) // 4 * 4
+        if res is None:
+            ap = _pad_identity(self._matrix(req), n4)
+            res = _Resident(ap, qr=mixed.qr_square_tf32(ap), split=mixed.split_matrix(ap))
+            self._publish(req.op_id, "qr_mixed", req.n, res)
+        ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
+                            inner_max_steps=5, restart=8, split=res.split, qr=res.qr,
+                            arith="auto", fallback=True)
+        x = ir.x[:, : req.n].contiguous()
+        return Completion(req.rid, x, max(ir.berr), "qr_mixed", ir.fallback, reused)
+
+    def _run_f64(self, req: Request, route: str) -> Completion:
+        """The plain FP64 GPU path of lineax's solvers: LU (getrf/getrs),
+        Cholesky (multi-CTA potrf, triangular solves) or Householder QR
+        (geqrf/ormqr/trsm), the factor resident for later requests."""
+        res = self._acquire(req.op_id)
+        reused = res is not None
+        if res is None:
             a = self._matrix(req)
-            lu, piv = _dense.lu_factor(a)
-            op = _F64Operator(a, lu, piv)
+            if route == "lu_f64":
+                lu, piv = _dense.lu_factor(a)
+                res = _Resident(a, lu=lu, piv=piv)
+            elif route == "chol_f64":
+                res = _Resident(a, u=_dense.cho_factor(a))
+            else:
+                res = _Resident(a, qr=_dense.geqrf(a))
+            self._publish(req.op_id, route, req.n, res)
         b = self._rhs(req)
-        x = _dense.lu_solve(op.lu, op.piv, b)
-        self.sched.remember(req.op_id, resident_bytes("lu_f64", req.n), op)
-        return Completion(req.rid, x, float(_berr(op.a, x, b).max()), "lu_f64", False, reused)
-
-    def execute(self, batch: list) -> list:
-        """Serve one admitted batch (synchronises before returning)."""
-        groups = collections.defaultdict(list)
-        for r in batch:
-            groups[route_of(r.kind, r.n, self.mode)].append(r)
-        out = []
-        if groups["chol_ragged"]:
-            out += self._run_chol(groups["chol_ragged"])
-        if groups["lu_small"]:
-            out += self._run_small(groups["lu_small"])
-        for r in groups["lu_mixed"]:
-            out.append(self._run_mixed(r))
-        for r in groups["lu_f64"]:
-            out.append(self._run_f64(r))
-        torch.cuda.synchronize(self.device)
-        return out
+        if route == "lu_f64":
+            x = _dense.lu_solve(res.lu, res.piv, b)
+        elif route == "chol_f64":
+            x = _dense.cho_solve(res.u, b)
+        else:
+            x = mixed.qr_solve_f64(res.qr, b)
+        return Completion(req.rid, x, float(_berr(res.a, x, b).max()), route, False, reused)
 
     def _jobs(self, batch: list) -> list:
         """Admitted requests as jobs: one per ragged Cholesky group, one per
-        small-LU group, one per large request."""
+        small-LU group, one per other request."""
         groups = collections.defaultdict(list)
         for r in batch:
             groups[route_of(r.kind, r.n, self.mode)].append(r)
@@ -395,9 +516,21 @@ class SolveServer:
             jobs.append((self._run_small, groups["lu_small"]))
         for r in groups["lu_mixed"]:
             jobs.append((lambda rs: [self._run_mixed(rs[0])], [r]))
-        for r in groups["lu_f64"]:
-            jobs.append((lambda rs: [self._run_f64(rs[0])], [r]))
+        for r in groups["qr_mixed"]:
+            jobs.append((lambda rs: [self._run_qr_mixed(rs[0])], [r]))
+        for route in ("lu_f64", "chol_f64", "qr_f64"):
+            for r in groups[route]:
+                jobs.append((lambda rs, rt=route: [self._run_f64(rs[0], rt)], [r]))
         return jobs
+
+    def execute(self, batch: list) -> list:
+        """Serve one admitted batch on the current stream (synchronises
+        before returning)."""
+        out = []
+        for fn, reqs in self._jobs(batch):
+            out += fn(reqs)
+        torch.cuda.synchronize(self.device)
+        return out
 
     def _work(self, fn, reqs, t0: float):
         """One job on this worker thread's stream; returns its completions

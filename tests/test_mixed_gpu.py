@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from lineax_gb300 import batched
+from lineax_gb300 import _ffi, batched
 from oracle import dense
 
 pytestmark = pytest.mark.gpu
@@ -198,3 +198,48 @@ def test_mixed_edge_cases(dev):
     info2 = out.info.cpu().numpy()
     assert info2[2] == -2 and info2[1] == 0 and info2[3] == 0 and info2[0] == 0
     assert torch.equal(rb.system_b(out.x, 1), rb.system_b(res.x, 1))
+
+
+def test_mixed_factors_store_then_load_same_bits(dev):
+    """lxgb_posv_ragged_mixed_factors: a stored FP32 factor is the Cholesky
+    factor to FP32 accuracy, and solving again from it (no factorisation)
+    gives bit-identical solutions, iteration counts and backward errors."""
+    rng = np.random.default_rng(31)
+    ns, ks = [512, 300, 145, 144, 100, 16], [3, 8, 1, 2, 5, 4]
+    mats, rhs = make_ragged(rng, ns, ks)
+    rb = to_batch(mats, rhs, dev)
+    plain = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    store = [torch.empty((n, n), dtype=torch.float32, device=dev) for n in ns]
+    plan = batched.FactorPlan([batched.FACTOR_STORE] * len(ns), store, dev)
+    first = batched.spd_solve_ragged_mixed(rb, tol=TOL, factors=plan)
+    # a mix of loads and fresh factorisations in one launch
+    modes = [batched.FACTOR_LOAD, batched.FACTOR_COMPUTE, batched.FACTOR_LOAD,
+             batched.FACTOR_LOAD, batched.FACTOR_COMPUTE, batched.FACTOR_LOAD]
+    again = batched.spd_solve_ragged_mixed(
+        rb, tol=TOL, factors=batched.FactorPlan(modes, [f if m else None for m, f in
+                                                        zip(modes, store)], dev))
+    torch.cuda.synchronize()
+    for r in (first, again):
+        assert torch.equal(r.x, plain.x) and torch.equal(r.iters, plain.iters)
+        assert torch.equal(r.info, plain.info) and torch.equal(r.berr, plain.berr)
+    for s, n in enumerate(ns):
+        u = store[s].double().cpu().numpy()
+        u_ref = dense.cho_factor_upper(mats[s])
+        assert np.all(np.tril(u, -1) == 0)
+        assert np.abs(u - u_ref).max() <= 1e-4 * np.abs(u_ref).max()
+
+
+def test_mixed_factors_rejects_missing_pointers(dev):
+    rng = np.random.default_rng(32)
+    mats, rhs = make_ragged(rng, [20], [1])
+    rb = to_batch(mats, rhs, dev)
+    ws = batched.MixedWorkspace(rb.batch, rb.max_n, rb.max_nrhs, dev)
+    out = torch.empty_like(rb.b)
+    small = torch.empty(1, dtype=torch.int32, device=dev)
+    with pytest.raises(_ffi.LxgbError) as e:
+        _ffi.call("lxgb_posv_ragged_mixed_factors", rb.batch, rb.max_n, rb.max_nrhs,
+                  _ffi.ptr(rb.n), _ffi.ptr(rb.nrhs), _ffi.ptr(rb.a_off), _ffi.ptr(rb.a),
+                  _ffi.ptr(rb.b_off), _ffi.ptr(rb.b), _ffi.ptr(out), TOL, 10, _ffi.ptr(small),
+                  _ffi.ptr(small), _ffi.ptr(out), 0, 0, _ffi.ptr(ws.buf), ws.nbytes,
+                  _ffi.stream_handle(dev))
+    assert e.value.status == 100

@@ -181,3 +181,27 @@ def test_gmres_ir_through_linear_solve(dev):
     x_ref, r_ref, s_ref = krylov.gmres(lambda v: a @ v, b, rtol=1e-10, atol=1e-10, precond=pre)
     # The inverses carry FP32 rounding of their own: allow two restart cycles
     assert r_ref == 0 and abs(sol.stats["num_steps"] - s_ref) <= 2
+
+
+@pytest.mark.parametrize("n,cond,precision,max_outer", [(1024, 1e2, "3xtf32", 20),
+                                                        (512, 1e6, "tf32", 6),
+                                                        (768, 1e6, "3xtf32", 20)])
+def test_gmres_ir_single_call_equals_host_loop(dev, n, cond, precision, max_outer):
+    """lxgb_gmres_ir_run (the refinement loop, its tier switch and the inner
+    GMRES loop as conditional graph nodes on the device) issues the host
+    loop's kernels in the host loop's order: the same solution bits, the same
+    number of refinement steps and the same backward errors, whether the
+    solve converges in the plain-refinement tier or moves on to GMRES."""
+    a = torch.tensor(conditioned(n, cond, n + 5), device=dev)
+    b = torch.tensor(np.random.default_rng(n).standard_normal((3, n)), device=dev)
+    f = mixed.lu_factor_tf32(a, precision)
+    inv = mixed.lu_inverse(f, precision)
+    sp = mixed.split_matrix(a)
+    kw = dict(tol=1e-12, restart=8, inner_max_steps=5, max_outer=max_outer, factor=f,
+              inverse=inv, split=sp, precision=precision, arith="auto", fallback=False)
+    host = mixed.gmres_ir(a, b, device_loop=False, **kw)
+    devl = mixed.gmres_ir(a, b, device_loop=True, **kw)
+    assert torch.equal(host.x, devl.x)
+    assert host.outer == devl.outer and host.converged == devl.converged
+    assert host.berr == devl.berr
+    assert (max(host.inner_steps) > 0) == (max(devl.inner_steps) > 0)

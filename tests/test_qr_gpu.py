@@ -121,3 +121,34 @@ def test_mixed_qr_through_linear_solve(dev):
     x_ref = np.linalg.lstsq(a, b, rcond=None)[0]
     assert sol.result == lx.RESULTS.successful
     assert np.abs(sol.value.cpu().numpy() - x_ref).max() <= 1e-10 * np.abs(x_ref).max()
+
+
+@pytest.mark.parametrize("n", [256, 1000, 2048])
+def test_square_tf32_qr_with_q_and_gmres_ir(dev, n):
+    """TF32 Householder QR that also forms Q (lxgb_geqrf_f32_tc_q): Q is
+    orthogonal and Q R reproduces A to TF32 accuracy; R^{-1} Qᵀ as the
+    GMRES-IR preconditioner recovers FP64 backward error on a square system
+    (the serving path of QR requests)."""
+    from lineax_gb300 import mixed
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n)) / np.sqrt(n) + np.eye(n)
+    b = rng.standard_normal((3, n))
+    qr = mixed.qr_square_tf32(t(a, dev))
+    qt = qr.qt.double().cpu().numpy()
+    rinv = qr.rinv.double().cpu().numpy()
+    # TF32 products (u = 2^-11): orthogonality and the factorisation hold to
+    # a small multiple of u
+    assert np.abs(qt @ qt.T - np.eye(n)).max() <= 2e-2
+    assert np.all(np.tril(rinv, -1) == 0)
+    r = np.linalg.inv(rinv)
+    assert np.abs(qt.T @ r - a).max() <= 2e-2 * np.abs(a).max()
+    res = mixed.gmres_ir(t(a, dev), t(b, dev), tol=1e-12, restart=8, inner_max_steps=5,
+                         arith="auto", qr=qr, fallback=False)
+    assert res.converged, res.berr
+    x = res.x.cpu().numpy()
+    be = dense.backward_errors_exact(a, x, b)
+    assert (be <= 1e-12 * (1 + 1e-4)).all(), be
+    # backward error 1e-12 bounds the forward error by about cond(A) 1e-12
+    bound = 4 * np.linalg.cond(a) * 1e-12
+    for c in range(3):
+        assert dense.forward_error(x[c], dense.qr_linear_solve(a, b[c])) <= bound

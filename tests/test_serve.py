@@ -17,7 +17,11 @@ def req(rid, kind, n, k=1, op=None, arrival=0.0, with_a=True):
 def test_routes():
     assert serve.route_of("cholesky", 1024, "mixed") == "chol_ragged"
     assert serve.route_of("cholesky", 1025, "mixed") == "lu_mixed"
-    assert serve.route_of("qr", 100, "mixed") == "lu_small"
+    assert serve.route_of("cholesky", 1025, "fp64") == "chol_f64"
+    assert serve.route_of("qr", 100, "mixed") == "qr_f64"   # QR requests are served by QR
+    assert serve.route_of("qr", 169, "mixed") == "qr_mixed"
+    assert serve.route_of("qr", 4096, "fp64") == "qr_f64"
+    assert serve.route_of("lu", 100, "mixed") == "lu_small"
     assert serve.route_of("lu", 169, "fp64") == "lu_f64"
     with pytest.raises(ValueError):
         serve.route_of("svd", 10, "mixed")
