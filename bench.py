@@ -1072,13 +1072,15 @@ def main():
                    help="time the plain FP64 LU at every condition number (gmres_ir)")
     args = p.parse_args()
     COUNT = args.systems
-    if args.workload == "gmres_ir":
-        run_gmres_ir(args)
-        return
-    if args.workload in ("lu_batch", "qr_ls", "cg_poisson", "serve", "peaks", "cholesky_large"):
-        {"lu_batch": run_lu_batch, "qr_ls": run_qr_ls, "cg_poisson": run_cg_poisson,
-         "serve": run_serve, "peaks": run_peaks,
-         "cholesky_large": run_cholesky_large}[args.workload](args)
+    modes = {"gmres_ir": run_gmres_ir, "lu_batch": run_lu_batch, "qr_ls": run_qr_ls,
+             "cg_poisson": run_cg_poisson, "serve": run_serve, "peaks": run_peaks,
+             "cholesky_large": run_cholesky_large}
+    if args.workload in modes:
+        # every secondary workload's lines come with the clocks sampled while it ran
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            modes[args.workload](args)
+        print(json.dumps({"workload": args.workload, "phase": "clocks",
+                          "clocks": clk.summary()}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -149,6 +149,8 @@ struct MxSmem {
   int done[kMxKc];
   int next;
   int flag;
+  int tcstat;                     // status of the tensor-core update (0 or -3)
+  unsigned tcphase;               // completed phases of tcbar
   unsigned tmem;                  // tensor-memory accumulator (128 columns) of the update
   alignas(8) unsigned long long tcbar;  // completion of the update's MMAs
 };
@@ -236,12 +238,21 @@ template <int NBMAX>
 __device__ __noinline__ int warp_potrf_block(float* F, int64_t ld, int j0, int nb, float* rd, float* ublk,
                                              float* linv) {
   const int lane = threadIdx.x & 31;
+  const int ldi = (int)ld;
+  float* base = F + (int64_t)j0 * ld + j0 + lane;  // row i of the block at base + i * ldi
   float col[NBMAX];
 #pragma unroll
   for (int i = 0; i < NBMAX; ++i) {
     const bool in = (i < nb) && (i <= lane) && (lane < nb);
-    col[i] = in ? F[(int64_t)(j0 + i) * ld + j0 + lane] : ((i == lane) ? 1.0f : 0.0f);
+    col[i] = in ? base[i * ldi] : ((i == lane) ? 1.0f : 0.0f);
   }
+  // Linv = U_JJ^{-T} in the same loop: lane j carries column j of Linv, z_k =
+  // (e_k - sum_{q<k} U[q][k] z_q) / U[k][k], whose sums acc[k] grow by
+  // U[k][i] z_k as each row k of U is broadcast for the rank-1 update — no
+  // second pass of dependent substitutions.
+  float acc[NBMAX];
+#pragma unroll
+  for (int i = 0; i < NBMAX; ++i) acc[i] = 0.0f;
   int bad = 0;
 #pragma unroll
   for (int k = 0; k < NBMAX; ++k) {
@@ -251,32 +262,18 @@ __device__ __noinline__ int warp_potrf_block(float* F, int64_t ld, int j0, int n
     const float r = 1.0f / d;
     col[k] = (lane == k) ? d : ((lane > k) ? col[k] * r : col[k]);
     if (lane == 0 && k < nb) rd[k] = r;
+    const float zk = (((lane == k) ? 1.0f : 0.0f) - acc[k]) * r;
+    if (lane < NBMAX) linv[k * (NBMAX + 1) + lane] = zk;
 #pragma unroll
     for (int i = k + 1; i < NBMAX; ++i) {
       const float uki = __shfl_sync(0xffffffffu, col[k], i);
       col[i] = (lane >= i) ? fmaf(-uki, col[k], col[i]) : col[i];
+      acc[i] = fmaf(uki, zk, acc[i]);
     }
   }
 #pragma unroll
-  for (int i = 0; i < NBMAX; ++i) {
-    if (lane < NBMAX) ublk[i * (NBMAX + 1) + lane] = col[i];
-    if (bad == 0 && i < nb && i <= lane && lane < nb) F[(int64_t)(j0 + i) * ld + j0 + lane] = col[i];
-  }
-  __syncwarp();
-  // Linv = U_JJ^{-T}: lane j solves U_JJᵀ z = e_j (z[p] = 0 for p < j) and
-  // stores z as column j of Linv.
-  if (lane < NBMAX) {
-    float z[NBMAX];
-#pragma unroll
-    for (int p = 0; p < NBMAX; ++p) {
-      float v = (p == lane) ? 1.0f : 0.0f;
-#pragma unroll
-      for (int q = 0; q < p; ++q) v = fmaf(-ublk[q * (NBMAX + 1) + p], z[q], v);
-      z[p] = v / ublk[p * (NBMAX + 1) + p];
-    }
-#pragma unroll
-    for (int p = 0; p < NBMAX; ++p) linv[p * (NBMAX + 1) + lane] = z[p];
-  }
+  for (int i = 0; i < NBMAX; ++i)
+    if (bad == 0 && i < nb && i <= lane && lane < nb) base[i * ldi] = col[i];
   __syncwarp();
   return bad;
 }
@@ -288,16 +285,18 @@ __device__ __noinline__ int warp_potrf_block(float* F, int64_t ld, int j0, int n
 template <int NBMAX>
 __device__ __noinline__ void block_row_trsm(float* F, int64_t ld, int kb, int nb, int j_lo, int n,
                                             const float* linv) {
+  const int ldi = (int)ld;  // 32-bit row offsets: one base address per column
   for (int j = j_lo + threadIdx.x; j < n; j += blockDim.x) {
+    float* col = F + (int64_t)kb * ld + j;
     float a[NBMAX];
 #pragma unroll
-    for (int p = 0; p < NBMAX; ++p) a[p] = (p < nb) ? F[(int64_t)(kb + p) * ld + j] : 0.0f;
+    for (int p = 0; p < NBMAX; ++p) a[p] = (p < nb) ? col[p * ldi] : 0.0f;
 #pragma unroll
     for (int p = 0; p < NBMAX; ++p) {
-      float y = 0.0f;
+      float y[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // four chains instead of one
 #pragma unroll
-      for (int q = 0; q <= p; ++q) y = fmaf(linv[p * (NBMAX + 1) + q], a[q], y);
-      if (p < nb) F[(int64_t)(kb + p) * ld + j] = y;
+      for (int q = 0; q <= p; ++q) y[q & 3] = fmaf(linv[p * (NBMAX + 1) + q], a[q], y[q & 3]);
+      if (p < nb) col[p * ldi] = (y[0] + y[1]) + (y[2] + y[3]);
     }
   }
 }
@@ -401,26 +400,31 @@ static_assert(sizeof(TcBands) == 4 * kTcBandFloats * 4, "band layout");
 // Rows [128 band, +128) of Wᵀ (Wᵀ[i][p] = U[j0+p][t0+i], zero for p >= nb or
 // i >= m) into hi/lo: row r is 128 bytes, 16-byte granule g of row r at
 // position g ^ (r & 7) — the layout smem_desc_sw128 describes.
+// Stages band `band` with the threads [t_lo, t_lo + nthr) of the CTA.
 __device__ __forceinline__ void tc_stage_band(const float* __restrict__ U, int ldu, int j0, int nb,
-                                              int t0, int m, int band, float* hi, float* lo) {
-  // 1024 (row, granule) pairs over 256 threads: all loads first, then the
-  // splits and the shared-memory stores (the loads stay in flight together)
-  constexpr int kPer = (kTcBand * 8) / kMxThreads;
-  float v[kPer][4];
+                                              int t0, int m, int band, float* hi, float* lo,
+                                              int t_lo, int nthr) {
+  const int me = threadIdx.x - t_lo;
+  // all loads first, then the splits and the shared-memory stores, so the
+  // loads of one thread are in flight together
+  constexpr int kMaxPer = (kTcBand * 8 + 223) / 224;
+  float v[kMaxPer][4];
 #pragma unroll
-  for (int it = 0; it < kPer; ++it) {
-    const int e = threadIdx.x + it * kMxThreads;
+  for (int it = 0; it < kMaxPer; ++it) {
+    const int e = me + it * nthr;
     const int r = e & (kTcBand - 1), g = e >> 7;
     const int i = band * kTcBand + r;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int p = 4 * g + q;
-      v[it][q] = (i < m && p < nb) ? __ldg(U + (int64_t)(j0 + p) * ldu + t0 + i) : 0.0f;
+      v[it][q] = (e < kTcBand * 8 && i < m && p < nb) ? __ldg(U + (int64_t)(j0 + p) * ldu + t0 + i)
+                                                      : 0.0f;
     }
   }
 #pragma unroll
-  for (int it = 0; it < kPer; ++it) {
-    const int e = threadIdx.x + it * kMxThreads;
+  for (int it = 0; it < kMaxPer; ++it) {
+    const int e = me + it * nthr;
+    if (e >= kTcBand * 8) break;
     const int r = e & (kTcBand - 1), g = e >> 7;
     float4 h, l;
     h.x = round_tf32(v[it][0]); l.x = round_tf32(v[it][0] - h.x);
@@ -433,22 +437,52 @@ __device__ __forceinline__ void tc_stage_band(const float* __restrict__ U, int l
   }
 }
 
-// Returns 0, or -3 if an MMA completion wait timed out (the factor is then
-// abandoned; a last bounded wait lets outstanding MMAs drain first).
+// Barrier over warps 1..7 (named barrier 1), with an OR of `flag`.
+__device__ __forceinline__ int bar_w17_or(int flag) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.s32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, 1, 224, q;\n\t"
+      "selp.s32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"(flag)
+      : "memory");
+  return r;
+}
+
+__device__ __forceinline__ void bar_w17() { asm volatile("bar.sync 1, 224;" ::: "memory"); }
+
+// The update of one trailing step on the tensor cores, and the factor of the
+// next diagonal block (rows/columns [t0, t0+32)).  Tile (0,0), which holds
+// that block, goes first with every warp; warp 0 then factors the block
+// (writing sm.flag) while warps 1..7 run the other tiles behind a named
+// barrier — warp 4 then reads TMEM lane quadrant 0 (rows 0..31 of a tile) for
+// both column halves.  Returns 0, or -3 if an MMA completion wait timed out
+// (after a last bounded wait that lets outstanding MMAs drain).
 __device__ __noinline__ int mx_update_tc(float* U, int ldu, int j0, int nb, int t0, int m,
                                          MxSmem& sm, TcBands& tb, unsigned& phase) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nbands = (m + kTcBand - 1) / kTcBand;
   constexpr unsigned idesc = idesc_tf32(kTcBand, kTcBand);
-  for (int ti = 0; ti < nbands; ++ti) {
-    tc_stage_band(U, ldu, j0, nb, t0, m, ti, tb.ah, tb.al);
-    for (int tj = ti; tj < nbands; ++tj) {
+  if (tid == 0) sm.tcstat = 0;
+  int t = 0;
+  bool out = false;  // warp 0 leaves the tile loop after tile (0,0)
+  for (int ti = 0; ti < nbands && !out; ++ti) {
+    for (int tj = ti; tj < nbands; ++tj, ++t) {
+      const bool solo = t > 0;  // warps 1..7 only from the second tile on
+      if (solo && warp == 0) {
+        out = true;
+        break;
+      }
+      const int t_lo = solo ? 32 : 0, nthr = solo ? 224 : 256;
       const bool same = tj == ti;
-      if (!same) tc_stage_band(U, ldu, j0, nb, t0, m, tj, tb.bh, tb.bl);
+      if (t == 0 || tj == ti) tc_stage_band(U, ldu, j0, nb, t0, m, ti, tb.ah, tb.al, t_lo, nthr);
+      if (!same) tc_stage_band(U, ldu, j0, nb, t0, m, tj, tb.bh, tb.bl, t_lo, nthr);
       // generic-proxy smem writes -> visible to the tensor core's async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
+      if (solo) bar_w17(); else __syncthreads();
+      if (tid == t_lo) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const float* bh = same ? tb.ah : tb.bh;
         const float* bl = same ? tb.al : tb.bl;
@@ -467,21 +501,25 @@ __device__ __noinline__ int mx_update_tc(float* U, int ldu, int j0, int nb, int 
       __syncwarp();
       const bool ok = mbar_wait(&sm.tcbar, phase & 1);
       ++phase;
-      // one decision for the whole CTA (a wait could end differently per thread)
-      const int timed_out = __syncthreads_or(!ok);
+      // one decision for every participating thread
+      const int timed_out = solo ? bar_w17_or(!ok) : __syncthreads_or(!ok);
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (timed_out) {
         if (!ok) mbar_wait(&sm.tcbar, (phase - 1) & 1);
-        __syncthreads();
-        return -3;
+        if (tid == t_lo) sm.tcstat = -3;
+        out = true;
+        break;
       }
-      // epilogue: warp w reads TMEM lanes 32 (w % 4).. (tile rows) and the
-      // column half w / 4
-      const int r = 32 * (warp & 3) + lane;
+      // epilogue: warp w reads TMEM lanes 32 (w % 4).. (tile rows); column
+      // half w / 4, or both halves for warp 4 while warp 0 is away
+      const int quad = warp & 3;
+      const int r = 32 * quad + lane;
       const int i = ti * kTcBand + r;
+      const int c_first = (solo && quad == 0) ? 0 : 64 * (warp >> 2);
+      const int c_count = (solo && quad == 0) ? 4 : 2;
 #pragma unroll 1
-      for (int cc = 0; cc < 2; ++cc) {
-        const int c0 = 64 * (warp >> 2) + 32 * cc;
+      for (int cc = 0; cc < c_count; ++cc) {
+        const int c0 = c_first + 32 * cc;
         const int jb = tj * kTcBand + c0;
         float* dst = U + (int64_t)(t0 + min(i, m - 1)) * ldu + t0 + jb;
         // the row's eight granules of C are loaded before anything is stored
@@ -493,7 +531,7 @@ __device__ __noinline__ int mx_update_tc(float* U, int ldu, int j0, int nb, int 
                                                     : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         float v[32];
-        tmem_ld32(sm.tmem + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)c0, v);
+        tmem_ld32(sm.tmem + ((unsigned)(32 * quad) << 16) + (unsigned)c0, v);
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
           const int col = jb + 4 * g;
@@ -507,10 +545,22 @@ __device__ __noinline__ int mx_update_tc(float* U, int ldu, int j0, int nb, int 
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();  // TMEM and the B band are free again
+      if (solo) bar_w17(); else __syncthreads();  // TMEM and the bands are free again
     }
   }
-  return 0;
+  __syncwarp();
+  if (warp == 0 && sm.tcstat == 0) {
+    // the next diagonal block, updated by tile (0,0), while the other warps
+    // finish the remaining tiles
+    const int bad = warp_potrf_block<kMxNB>(U, ldu, t0, min(kMxNB, m), sm.rd + t0, &sm.ublk[0][0],
+                                            &sm.linv[0][0]);
+    if (lane == 0) sm.flag = bad;
+  }
+  // warp 1 waited on every tile's commit: its phase count is everyone's now
+  if (tid == 32) sm.tcphase = phase;
+  __syncthreads();
+  phase = sm.tcphase;
+  return sm.tcstat;
 }
 
 __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float* U, int n, int ldu, MxSmem& sm,
@@ -537,17 +587,11 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
     block_row_trsm<kMxNB>(U, ldu, j0, nb, t0, n, &sm.linv[0][0]);
     __syncthreads();
     if (use_tc && m <= kMxStageCols) {
-      // tensor-core update, then the next diagonal block by warp 0
+      // tensor-core update, with the next diagonal block factored by warp 0
       TcBands& tb = *reinterpret_cast<TcBands*>(
           (reinterpret_cast<uintptr_t>(&st) + 1023) & ~static_cast<uintptr_t>(1023));
       const int rc = mx_update_tc(U, ldu, j0, nb, t0, m, sm, tb, phase);
       if (rc) return rc;
-      if (warp == 0) {
-        const int bad = warp_potrf_block<kMxNB>(U, ldu, t0, min(kMxNB, m), sm.rd + t0,
-                                                &sm.ublk[0][0], &sm.linv[0][0]);
-        if (lane == 0) sm.flag = bad;
-      }
-      __syncthreads();
       if (sm.flag) return sm.flag;
       continue;
     }

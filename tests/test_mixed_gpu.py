@@ -243,3 +243,30 @@ def test_mixed_factors_rejects_missing_pointers(dev):
                   _ffi.ptr(small), _ffi.ptr(out), 0, 0, _ffi.ptr(ws.buf), ws.nbytes,
                   _ffi.stream_handle(dev))
     assert e.value.status == 100
+
+
+@pytest.mark.parametrize("ns", [[145, 200, 300, 512, 400, 64], [544, 160, 33]])
+def test_mixed_tensor_core_update(dev, ns):
+    """The large-system factor's trailing updates on the tcgen05 tensor cores
+    (split TF32 products): every system reaches the 1e-12 backward error bar
+    and agrees with the oracle's solution, as with the CUDA-core updates."""
+    rng = np.random.default_rng(sum(ns) + 5)
+    ks = [1 + (5 * i) % 8 for i in range(len(ns))]
+    mats, rhs = make_ragged(rng, ns, ks)
+    rb = to_batch(mats, rhs, dev)
+    _ffi.call("lxgb_posv_mixed_set_tensor_cores", 1)
+    try:
+        res = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+        torch.cuda.synchronize()
+    finally:
+        _ffi.call("lxgb_posv_mixed_set_tensor_cores", 0)
+    ref = batched.spd_solve_ragged_mixed(rb, tol=TOL)
+    assert (res.info.cpu().numpy() == 0).all()
+    assert (res.iters.cpu().numpy() <= ref.iters.cpu().numpy() + 1).all()
+    for s, (m, r) in enumerate(zip(mats, rhs)):
+        xs = rb.system_b(res.x, s).cpu().numpy()
+        be = dense.backward_errors_exact(m, xs, r)
+        assert (be <= TOL * (1 + 1e-4)).all(), (ns[s], be)
+        x_ref = dense.cholesky_linear_solve(m, r.T).T
+        for c in range(ks[s]):
+            assert dense.forward_error(xs[c], x_ref[c]) <= 1e-9
