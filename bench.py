@@ -454,7 +454,8 @@ def haar_conditioned(n, cond, seed, dev):
 
 def run_gmres_ir(args):
     """Dense n×n, 16 right-hand sides, cond in {1e2, 1e6, 1e10}: FP32 LU with
-    TF32 or 3xTF32 tensor-core updates + GMRES-IR to backward error <= 1e-12,
+    BF16, TF32 or 3xTF32 tensor-core updates + GMRES-IR to backward error <= 1e-12
+    (a stalled factor escalates to the next precision before the FP64 LU),
     against the plain FP64 LU of this library.  One JSON line per case."""
     import time
 
@@ -475,7 +476,7 @@ def run_gmres_ir(args):
 
     # warm-up: module load and first-call costs of every kernel used below
     a0 = haar_conditioned(256, 1e2, 1, dev)
-    for prec in ("tf32", "3xtf32"):
+    for prec in ("bf16", "tf32", "3xtf32"):
         mixed.gmres_ir(a0, b[:, :256].contiguous(), precision=prec, restart=args.restart)
     lu0, piv0 = _dense.lu_factor(a0)
     _dense.lu_solve(lu0, piv0, b[:, :256].contiguous())
@@ -522,7 +523,8 @@ def run_gmres_ir(args):
             e[3].record()
             res = mixed.gmres_ir(a, b, tol=1e-12, restart=args.restart, max_outer=20,
                                  inner_max_steps=args.inner_max_steps, factor=f, inverse=inv,
-                                 split=sp, precision=prec, arith=args.arith, fallback=True)
+                                 split=sp, precision=prec, arith=args.arith, fallback=True,
+                                 escalate=args.arith == "auto")
             e[4].record()
             torch.cuda.synchronize()
             total = e[0].elapsed_time(e[4])
@@ -533,6 +535,8 @@ def run_gmres_ir(args):
                   "total_ms": total, "outer": res.outer, "inner_cycles": res.inner_steps,
                   "max_berr": max(res.berr), "converged": res.converged,
                   "fp64_fallback": res.fallback,
+                  "tiers": [{"factor": t[0], "outer": t[1], "converged": t[2]}
+                            for t in res.tiers],
                   "solves_per_s": k / (total * 1e-3), "wall_s": time.perf_counter() - t0})
             del f, inv, sp, res
             torch.cuda.empty_cache()
@@ -909,8 +913,12 @@ def serve_suite(args, dev, loads=(0.25, 0.5, 0.75), emit=None):
     emit = emit or (lambda obj: None)
     tag = f"serve_{count}req_n32-{args.serve_nmax}"
     with ClockSampler(dev.index or 0) as clk:
+        # warm-up: one untimed pass of each server over the timed request
+        # stream itself, so neither pays first-use costs (kernel loading, the
+        # allocator's first blocks of large orders) inside its timing
         for mode in ("mixed", "fp64"):
             serve.SolveServer(dev, mode=mode).run(warm, realtime=False)
+            one(mode, None, 5)
         torch.cuda.synchronize()
         sat = {m: one(m, None, 5) for m in ("fp64", "mixed")}
         for m in ("fp64", "mixed"):
@@ -1066,7 +1074,9 @@ def main():
     p.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget (serve)")
     p.add_argument("--arith", default="auto", choices=["auto", "df", "fp32"],
                    help="inner GMRES arithmetic (gmres_ir)")
-    p.add_argument("--precisions", default="tf32,3xtf32", help="factor precisions (gmres_ir)")
+    p.add_argument("--precisions", default="bf16,tf32,3xtf32",
+                   help="first factor precision of each case (gmres_ir; a stalled factor "
+                        "escalates bf16 -> tf32 -> 3xtf32 -> FP64)")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 LU line (gmres_ir)")
     p.add_argument("--fp64-all", action="store_true",
                    help="time the plain FP64 LU at every condition number (gmres_ir)")

@@ -496,10 +496,20 @@ int lxgb_gemm_3xtf32_nt(int32_t m, int32_t n, int32_t k, const float* a,
                         const float* b_lo, int64_t ldb, float* c, int64_t ldc,
                         float alpha, float beta, int32_t* err, void* stream);
 
+/* C = alpha * A Bᵀ + beta * C on the tcgen05 tensor cores with BF16 inputs
+ * (A m×k, B n×k, __nv_bfloat16 row-major, k contiguous; lda, ldb multiples
+ * of 8, 16-byte aligned) and FP32 accumulation; C FP32 row-major.  *err as for
+ * lxgb_gemm_tf32_nt.  The trailing update of the BF16 factor tier of the
+ * mixed-precision LU (lineax/_solver/lu.py:53). */
+int lxgb_gemm_bf16_nt(int32_t m, int32_t n, int32_t k, const void* a, int64_t lda,
+                      const void* b, int64_t ldb, float* c, int64_t ldc, float alpha,
+                      float beta, int32_t* err, void* stream);
+
 /* Mixed-precision LU for GMRES-IR: P A = L U in FP32 with partial pivoting
  * (first row of max |a|), 64-column panels, trailing updates on the tcgen05
  * tensor cores with FP32 accumulation: precision 0 = TF32 products, 1 =
- * 3xTF32 (hi/lo operand split, FP32-level accuracy).  If a64 is not NULL the
+ * 3xTF32 (hi/lo operand split, FP32-level accuracy), 2 = BF16 products
+ * (L21 and U12 rounded to BF16 for each update, tcgen05 kind::f16).  If a64 is not NULL the
  * row-major FP64 matrix is first rounded into lu (n×n FP32, 16-byte aligned);
  * otherwise lu already holds the FP32 matrix.  n must be a multiple of 4.
  * piv: 0-based swaps; info as getrf; *err (device, zeroed by the caller) = 1

@@ -62,6 +62,8 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "lxgb_gmres_ir_run": (ctypes.c_int, [c_i32, c_i64, c_p, c_p, c_p, c_p, c_p, c_f64, c_f64,
                                          c_i32, c_i32, c_i32, c_i32, c_i32, c_p, c_p, c_p, c_i64,
                                          c_p]),
+    "lxgb_gemm_bf16_nt": (ctypes.c_int, [c_i32, c_i32, c_i32, c_p, c_i64, c_p, c_i64, c_p, c_i64,
+                                         ctypes.c_float, ctypes.c_float, c_p, c_p]),
     "lxgb_posv_ragged_mixed_noalloc": (
         ctypes.c_int,
         [c_i64, c_i32, c_i32, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_f64, c_i32, c_p, c_p, c_p,

@@ -565,16 +565,19 @@ getrs_f32_kernel(int n, const float* __restrict__ lu, const int32_t* __restrict_
 
 using namespace lxgb;
 
-// Workspace: U12ᵀ (n×64), and for 3xTF32 the hi/lo splits of L21 and U12ᵀ.
+// Workspace: U12ᵀ (n×64), for 3xTF32 the hi/lo splits of L21 and U12ᵀ, for
+// BF16 the BF16 copies of L21 and U12ᵀ.
 extern "C" int64_t lxgb_getrf_f32_tc_workspace_size(int32_t n, int32_t precision) {
   const int64_t blk = (int64_t)(n > 0 ? n : 1) * kLu32NB * (int64_t)sizeof(float);
-  return 256 + (precision == 1 ? 5 : 1) * ((blk + 255) & ~(int64_t)255);
+  const int blocks = precision == 1 ? 5 : (precision == 2 ? 4 : 1);
+  return 256 + blocks * ((blk + 255) & ~(int64_t)255);
 }
 
 extern "C" int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_t* piv,
                                  int32_t* info, int32_t precision, int32_t* err, void* work,
                                  int64_t work_bytes, void* stream) {
-  LXGB_REQUIRE(precision == 0 || precision == 1, "getrf_f32_tc: precision must be 0 or 1");
+  LXGB_REQUIRE(precision >= 0 && precision <= 2,
+               "getrf_f32_tc: precision must be 0 (TF32), 1 (3xTF32) or 2 (BF16)");
   LXGB_REQUIRE(n >= 0, "getrf_f32_tc: negative size");
   if (n == 0) return LXGB_SUCCESSFUL;
   LXGB_REQUIRE(lu && piv && info && err && work, "getrf_f32_tc: null pointer");
@@ -620,6 +623,12 @@ extern "C" int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_
         if (!rc)
           rc = gemm_tf32_nt_split(n2, n2, nb, ah, al, kLu32NB, bh, bl, kLu32NB, c22, n, -1.0f, 1.0f,
                                   err, st);
+      } else if (precision == 2) {
+        // BF16 operands (8-bit significands), FP32 accumulation in tensor memory
+        rc = bf16_convert(n2, nb, l21, n, ah, kLu32NB, st);
+        if (!rc) rc = bf16_convert(n2, nb, bt, kLu32NB, bh, kLu32NB, st);
+        if (!rc)
+          rc = gemm_bf16_nt(n2, n2, nb, ah, kLu32NB, bh, kLu32NB, c22, n, -1.0f, 1.0f, err, st);
       } else {
         rc = gemm_tf32_nt(n2, n2, nb, l21, n, bt, kLu32NB, c22, n, -1.0f, 1.0f, err, st);
       }

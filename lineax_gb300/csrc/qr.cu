@@ -22,6 +22,7 @@
 #include <math.h>
 
 #include <map>
+#include <type_traits>
 #include <mutex>
 #include <utility>
 
@@ -336,7 +337,176 @@ qr_panel_cluster_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
   cluster.sync();  // CTA 0 has finished reading the others' shared memory
 }
 
-template <typename T, bool SM>
+// FP32 panel with one cluster barrier per column (the panel of the
+// mixed-precision QR).  The norm of column k below the diagonal and the dots
+// d_q = a_kᵀ a_q of every trailing column q come out of one pass and one
+// cluster-wide reduction; with scal = 1 / (alpha - beta), the reflector's
+// dots are w_q = a_q[k] + scal d_q and the update is a_q[i] -= tau w_q scal a_k[i]
+// (i > k), a_q[k] -= tau w_q — the same reflectors as larfg/larf, with one
+// reduction per column instead of two.  Rows stay in shared memory for the
+// whole panel.  Partials are double-buffered by column parity: a CTA can only
+// overwrite a buffer after every CTA has passed the barrier of the column
+// that read it.
+__global__ void __launch_bounds__(kQrCluThreads, 1)
+qr_panel_cluster_f32_kernel(int64_t mm, int j0, int pe, int64_t rows_per_cta,
+                            float* __restrict__ h, float* __restrict__ tau,
+                            float* __restrict__ t_out) {
+  extern __shared__ __align__(16) unsigned char qr_dyn[];
+  __shared__ float p_d[2][kQrNB + 1];   // [0]: |a_k below k|^2, [1 + q]: a_kᵀ a_q
+  __shared__ float p_row[2][kQrNB + 1]; // the owner's row k: [0] alpha, [1 + q] a_q[k]
+  __shared__ float G[kQrNB][kQrNB + 1];
+  __shared__ float Tm[kQrNB][kQrNB + 1];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int ncta = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int nb = pe - j0;
+  const int64_t r_lo = j0 + (int64_t)rank * rows_per_cta;
+  const int64_t r_hi = min(mm, r_lo + rows_per_cta);
+  float* S = reinterpret_cast<float*>(qr_dyn);
+  auto at = [&](int q, int64_t i) -> float& { return S[(int64_t)q * rows_per_cta + (i - r_lo)]; };
+  for (int q = 0; q < nb; ++q)
+    for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) at(q, i) = h[(int64_t)(j0 + q) * mm + i];
+  __syncthreads();
+  for (int k = j0; k < pe; ++k) {
+    const int par = (k - j0) & 1;
+    const int kk = k - j0;
+    const bool own_k = (k >= r_lo && k < r_hi);
+    const int nrem = pe - k - 1;
+    const int64_t i_lo = max((int64_t)k + 1, r_lo);
+    // pass 1: the norm (c = 0) and the trailing dots (c = 1 + q), one warp each
+    for (int c = warp; c <= nrem; c += nwarps) {
+      const int qq = c == 0 ? kk : kk + c;
+      int64_t i = i_lo + lane;
+      float a8[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) a8[u] = 0.0f;
+      for (; i + 7 * 32 < r_hi; i += 8 * 32) {
+        float vv[8], qv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { vv[u] = at(kk, i + 32 * u); qv[u] = at(qq, i + 32 * u); }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a8[u] = fmaf(vv[u], qv[u], a8[u]);
+      }
+      for (; i < r_hi; i += 32) a8[0] = fmaf(at(kk, i), at(qq, i), a8[0]);
+      float acc = ((a8[0] + a8[1]) + (a8[2] + a8[3])) + ((a8[4] + a8[5]) + (a8[6] + a8[7]));
+      acc = warp_sum(acc);
+      if (lane == 0) p_d[par][c] = acc;
+    }
+    if (own_k && tid <= nrem) p_row[par][tid] = at(kk + tid, k);
+    cluster.sync();
+    // every warp forms the reflector's scalars from the summed partials
+    const int own = (int)(kk / rows_per_cta);
+    float xn2 = (lane < ncta) ? cluster.map_shared_rank(&p_d[par][0], lane)[0] : 0.0f;
+    xn2 = warp_sum(xn2);
+    const float alpha = cluster.map_shared_rank(&p_row[par][0], own)[0];
+    const float xnorm = sqrtf(xn2);
+    float tk = 0.0f, scal = 1.0f, beta = alpha;
+    if (xnorm != 0.0f) {
+      beta = -copysignf(hypotf(alpha, xnorm), alpha);
+      tk = (beta - alpha) / beta;
+      scal = 1.0f / (alpha - beta);
+    }
+    if (tk != 0.0f) {
+      for (int q = warp; q < nrem; q += nwarps) {
+        float d = (lane < ncta) ? cluster.map_shared_rank(&p_d[par][0], lane)[1 + q] : 0.0f;
+        d = warp_sum(d);
+        const float aqk = cluster.map_shared_rank(&p_row[par][0], own)[1 + q];
+        const float w = fmaf(scal, d, aqk);
+        const float tw = tk * w;
+        const float tws = tw * scal;
+        const int qq = kk + 1 + q;
+        if (own_k && lane == 0) at(qq, k) = aqk - tw;
+        int64_t i = i_lo + lane;
+        for (; i + 7 * 32 < r_hi; i += 8 * 32) {
+          float vv[8], qv[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) { vv[u] = at(kk, i + 32 * u); qv[u] = at(qq, i + 32 * u); }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) at(qq, i + 32 * u) = fmaf(-tws, vv[u], qv[u]);
+        }
+        for (; i < r_hi; i += 32) at(qq, i) = fmaf(-tws, at(kk, i), at(qq, i));
+      }
+    }
+    __syncthreads();  // every trailing column has read the unscaled a_k
+    if (tk != 0.0f) {
+      for (int64_t i = i_lo + tid; i < r_hi; i += blockDim.x) at(kk, i) *= scal;
+      if (own_k && tid == 0) at(kk, k) = beta;
+    }
+    if (rank == 0 && tid == 0) tau[k] = tk;
+    __syncthreads();
+  }
+  // G[q][p] = v_qᵀ v_p (q < p) over this CTA's rows, summed in CTA 0; T by
+  // larft's recurrence (as in qr_panel_cluster_kernel)
+  {
+    __shared__ float Vc[64][kQrNB + 1];
+    int pq = -1, pp = -1;
+    for (int p2 = 1, t = 0; p2 < nb && pq < 0; ++p2) {
+      if (tid < t + p2) { pq = tid - t; pp = p2; }
+      t += p2;
+    }
+    float acc = 0.0f;
+    for (int64_t i0 = r_lo; i0 < r_hi; i0 += 64) {
+      for (int e = tid; e < 64 * kQrNB; e += blockDim.x) {
+        const int q = e / 64, ii = e % 64;
+        const int64_t i = i0 + ii;
+        Vc[ii][q] = (q < nb && i < r_hi)
+                        ? ((i < j0 + q) ? 0.0f : (i == j0 + q ? 1.0f : at(q, i)))
+                        : 0.0f;
+      }
+      __syncthreads();
+      if (pq >= 0) {
+#pragma unroll 8
+        for (int ii = 0; ii < 64; ++ii) acc = fmaf(Vc[ii][pq], Vc[ii][pp], acc);
+      }
+      __syncthreads();
+    }
+    if (pq >= 0) G[pq][pp] = acc;
+  }
+  cluster.sync();
+  if (rank == 0) {
+    __shared__ float Gs[kQrNB][kQrNB + 1];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int q = e / nb, pp2 = e % nb;
+      float g = 0.0f;
+      if (q < pp2)
+        for (int c = 0; c < ncta; ++c) g += cluster.map_shared_rank(&G[0][0], c)[q * (kQrNB + 1) + pp2];
+      Gs[q][pp2] = g;
+    }
+    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x) Tm[e / kQrNB][e % kQrNB] = 0.0f;
+    __syncthreads();
+    if (warp == 0) {
+      for (int k = 0; k < nb; ++k) {
+        const float tkk = tau[j0 + k];
+        float v = 0.0f;
+        if (lane < k) {
+          for (int q = lane; q < k; ++q) v = fmaf(Tm[lane][q], Gs[q][k], v);
+          v = -tkk * v;
+        }
+        __syncwarp();
+        if (lane < k) Tm[lane][k] = v;
+        if (lane == k) Tm[k][k] = tkk;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
+      t_out[e] = Tm[e / kQrNB][e % kQrNB];
+  }
+  for (int q = 0; q < nb; ++q)
+    for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) h[(int64_t)(j0 + q) * mm + i] = at(q, i);
+  cluster.sync();  // CTA 0 has finished reading the others' shared memory
+}
+
+// The panel kernel a launch uses: the FP32 single-barrier variant (FUSED,
+// rows in shared memory), or qr_panel_cluster_kernel<T, SM>.
+template <typename T, bool SM, bool FUSED>
+static const void* qr_panel_fn() {
+  if constexpr (FUSED) return reinterpret_cast<const void*>(qr_panel_cluster_f32_kernel);
+  return reinterpret_cast<const void*>(qr_panel_cluster_kernel<T, SM>);
+}
+
+template <typename T, bool SM, bool FUSED>
 static bool qr_cluster_fits(int c, size_t smem) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, bool> known;
@@ -346,11 +516,10 @@ static bool qr_cluster_fits(int c, size_t smem) {
   const auto key = std::make_pair(dev, c * 1000000 + (int)(smem >> 8));
   auto it = known.find(key);
   if (it != known.end()) return it->second;
-  bool ok = cudaFuncSetAttribute(qr_panel_cluster_kernel<T, SM>,
-                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
-  if (ok && smem > 0)
-    ok = ensure_dynamic_smem(reinterpret_cast<const void*>(qr_panel_cluster_kernel<T, SM>),
-                             (int)smem) == cudaSuccess;
+  const void* fn = qr_panel_fn<T, SM, FUSED>();
+  bool ok = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess;
+  if (ok && smem > 0) ok = ensure_dynamic_smem(fn, (int)smem) == cudaSuccess;
   if (ok) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)c);
@@ -364,19 +533,17 @@ static bool qr_cluster_fits(int c, size_t smem) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel<T, SM>, &cfg) ==
-             cudaSuccess &&
-         nclusters >= 1;
+    ok = cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) == cudaSuccess && nclusters >= 1;
   }
   if (!ok) cudaGetLastError();
   known[key] = ok;
   return ok;
 }
 
-template <typename T, bool SM>
+template <typename T, bool SM, bool FUSED>
 static int launch_qr_panel_variant(int c, int64_t r, size_t smem, int64_t mm, int j0, int pe,
                                    T* h, T* tau, T* t_out, cudaStream_t st) {
-  if (!qr_cluster_fits<T, SM>(c, smem)) return -1;
+  if (!qr_cluster_fits<T, SM, FUSED>(c, smem)) return -1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c);
   cfg.blockDim = dim3(kQrCluThreads);
@@ -389,8 +556,12 @@ static int launch_qr_panel_variant(int c, int64_t r, size_t smem, int64_t mm, in
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel<T, SM>, mm, j0, pe, r, h, tau, t_out) !=
-      cudaSuccess) {
+  cudaError_t e;
+  if constexpr (FUSED)
+    e = cudaLaunchKernelEx(&cfg, qr_panel_cluster_f32_kernel, mm, j0, pe, r, h, tau, t_out);
+  else
+    e = cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel<T, SM>, mm, j0, pe, r, h, tau, t_out);
+  if (e != cudaSuccess) {
     cudaGetLastError();
     return -1;
   }
@@ -398,7 +569,8 @@ static int launch_qr_panel_variant(int c, int64_t r, size_t smem, int64_t mm, in
 }
 
 // 0 when the cluster kernel was launched, -1 when the caller must fall back.
-// The panel's rows stay in shared memory when a CTA's slice fits (FP32).
+// The panel's rows stay in shared memory when a CTA's slice fits; the FP32
+// factor then takes the single-barrier panel.
 template <typename T>
 static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* t_out,
                                    cudaStream_t st) {
@@ -407,10 +579,15 @@ static int launch_qr_panel_cluster(int64_t mm, int j0, int pe, T* h, T* tau, T* 
   c = c < 1 ? 1 : (c > kQrCluMax ? kQrCluMax : c);
   const int64_t r = (rows + c - 1) / c;
   const size_t slice = (size_t)kQrNB * r * sizeof(T);
-  if (slice <= 160 * 1024 &&
-      launch_qr_panel_variant<T, true>(c, r, slice, mm, j0, pe, h, tau, t_out, st) == 0)
-    return 0;
-  return launch_qr_panel_variant<T, false>(c, r, 0, mm, j0, pe, h, tau, t_out, st);
+  if (slice <= 160 * 1024) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (launch_qr_panel_variant<T, true, true>(c, r, slice, mm, j0, pe, h, tau, t_out, st) == 0)
+        return 0;
+    }
+    if (launch_qr_panel_variant<T, true, false>(c, r, slice, mm, j0, pe, h, tau, t_out, st) == 0)
+      return 0;
+  }
+  return launch_qr_panel_variant<T, false, false>(c, r, 0, mm, j0, pe, h, tau, t_out, st);
 }
 
 // T (nb×nb, upper) of panel rows [j0, j0+nb): T[k][k] = tau_k and
@@ -812,30 +989,26 @@ __global__ void qr32_make_v_kernel(int64_t mm, int j0, int nb, const float* __re
   }
 }
 
-// w2[j][p] = sum_q (sum_s wpart[s][j][q]) T[q][p], j < n2.
-__global__ void qr32_wt_kernel(int n2, int nb, int splits, const float* __restrict__ wpart,
-                               const float* __restrict__ T, float* __restrict__ w2) {
+// w2[j][p] = sum_q (sum_s wpart[s][j][q]) T[q][p], j < n2: one warp per row
+// j, lane q sums the K-split partials of W[j][q] (coalesced), then lane p
+// forms its output from W[j][·] broadcast by shuffles.
+__global__ void __launch_bounds__(256)
+qr32_wt_kernel(int n2, int nb, int splits, const float* __restrict__ wpart,
+               const float* __restrict__ T, float* __restrict__ w2) {
   __shared__ float Ts[kQrNB][kQrNB + 1];
   for (int e = threadIdx.x; e < kQrNB * kQrNB; e += blockDim.x)
     Ts[e / kQrNB][e % kQrNB] = T[e];
   __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (j >= n2) return;
-  float w[kQrNB];
+  float w = 0.0f;
+  if (lane < nb)
+    for (int sp = 0; sp < splits; ++sp) w += wpart[((int64_t)sp * n2 + j) * kQrNB + lane];
+  float a = 0.0f;
 #pragma unroll
-  for (int q = 0; q < kQrNB; ++q) w[q] = 0.0f;
-  for (int sp = 0; sp < splits; ++sp) {
-#pragma unroll
-    for (int q = 0; q < kQrNB; ++q)
-      if (q < nb) w[q] += wpart[((int64_t)sp * n2 + j) * kQrNB + q];
-  }
-#pragma unroll
-  for (int p = 0; p < kQrNB; ++p) {
-    float a = 0.0f;
-#pragma unroll
-    for (int q = 0; q < kQrNB; ++q) a = fmaf(w[q], Ts[q][p], a);
-    w2[(int64_t)j * kQrNB + p] = (p < nb) ? a : 0.0f;
-  }
+  for (int q = 0; q < kQrNB; ++q) a = fmaf(__shfl_sync(0xffffffffu, w, q), Ts[q][lane], a);
+  w2[(int64_t)j * kQrNB + lane] = (lane < nb) ? a : 0.0f;
 }
 
 __global__ void qr32_transpose_cvt_kernel(int64_t rows, int64_t cols, const double* __restrict__ a,
@@ -914,17 +1087,12 @@ static int geqrf_f32_tc_driver(int64_t m, int64_t n, const double* a, float* h, 
   auto apply = [&](float* c, int rows, int j0, int nb, const float* Tp) -> int {
     const int64_t klen = m - j0;
     const int64_t chunk = ((klen + kQr32Split - 1) / kQr32Split + 31) / 32 * 32;
-    int used = 0;
-    for (int sp = 0; sp < kQr32Split; ++sp) {
-      const int64_t k0 = j0 + (int64_t)sp * chunk;
-      if (k0 >= m) break;
-      const int64_t kl = min(chunk, m - k0);
-      int rc = gemm_tf32_nt(rows, nb, (int)kl, c + k0, m, vrows + k0, m,
-                            wpart + (int64_t)sp * rows * kQrNB, kQrNB, 1.0f, 0.0f, err, st);
-      if (rc) return rc;
-      ++used;
-    }
-    qr32_wt_kernel<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(rows, nb, used, wpart, Tp, w2);
+    const int used = (int)((klen + chunk - 1) / chunk);
+    // W partials over `used` K ranges in one split-K launch
+    int rc0 = gemm_tf32_nt_splitk(rows, nb, (int)klen, c + j0, m, vrows + j0, m, wpart, kQrNB,
+                                  (int)chunk, used, err, st);
+    if (rc0) return rc0;
+    qr32_wt_kernel<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(rows, nb, used, wpart, Tp, w2);
     return gemm_tf32_nt(rows, (int)klen, nb, w2, kQrNB, vcols + (int64_t)j0 * kQrNB, kQrNB,
                         c + j0, m, -1.0f, 1.0f, err, st);
   };

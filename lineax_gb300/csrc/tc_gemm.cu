@@ -23,6 +23,8 @@
 #include "common.cuh"
 #include "tcgen05.cuh"
 
+#include <cuda_bf16.h>
+
 namespace lxgb {
 
 constexpr int kTcM = 128;
@@ -75,17 +77,25 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
                : "memory");
 }
 
-// SPLIT (3xTF32): A = Ah + Al and B = Bh + Bl with TF32-exact hi parts;
+// MODE 0: TF32 operands (FP32 in memory, read as TF32).
+// MODE 1 (3xTF32): A = Ah + Al and B = Bh + Bl with TF32-exact hi parts;
 // A Bᵀ ~= Ah Bhᵀ + Ah Blᵀ + Al Bhᵀ accumulated in the same tensor memory,
 // which restores FP32-level accuracy.
-template <bool SPLIT>
+// MODE 2: BF16 operands in memory (tcgen05.mma kind::f16, both operands
+// BF16, FP32 accumulation): a 128-byte shared-memory row holds 64 of them,
+// so a stage covers K = 64 with the same layout and 32-byte K steps.
+template <int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
 gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
                     const __grid_constant__ CUtensorMap map_b,
                     const __grid_constant__ CUtensorMap map_al,
                     const __grid_constant__ CUtensorMap map_bl,
                     const __grid_constant__ CUtensorMap map_c, int use_tma_c, int M, int N, int K,
-                    float* C, int64_t ldc, float alpha, float beta, int* err) {
+                    float* C, int64_t ldc, float alpha, float beta, int* err,
+                    int k_split_tiles, int64_t c_split_stride) {
+  constexpr bool SPLIT = MODE == 1;
+  constexpr bool BF = MODE == 2;
+  constexpr int kK = BF ? 2 * kTcK : kTcK;  // K elements per 128-byte stage row
   constexpr int kStages = SPLIT ? kTcStagesSplit : kTcStages;
   using Smem = TcSmem<kStages, SPLIT>;
   extern __shared__ unsigned char smem_raw[];
@@ -93,7 +103,15 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
-  const int ktiles = (K + kTcK - 1) / kTcK;
+  // split-K: CTA layer z takes k-tiles [z * k_split_tiles, ...) and writes its
+  // own C block at C + z * c_split_stride
+  int t_begin = 0;
+  int ktiles = (K + kK - 1) / kK;
+  if (k_split_tiles > 0) {
+    t_begin = (int)blockIdx.z * k_split_tiles;
+    ktiles = max(0, min(ktiles - t_begin, k_split_tiles));
+    C += (int64_t)blockIdx.z * c_split_stride;
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -123,16 +141,16 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
       if (!mbar_wait(&sm.empty[s], (r & 1) ^ 1)) { atomicExch(&sm.abort, 1); break; }
       if (*reinterpret_cast<volatile int*>(&sm.abort)) break;
       mbar_expect_tx(&sm.full[s], (SPLIT ? 4 : 2) * kTcTileBytes);
-      tma_load_2d(sm.a[s], &map_a, t * kTcK, m0, &sm.full[s]);
-      tma_load_2d(sm.b[s], &map_b, t * kTcK, n0, &sm.full[s]);
+      tma_load_2d(sm.a[s], &map_a, (t_begin + t) * kK, m0, &sm.full[s]);
+      tma_load_2d(sm.b[s], &map_b, (t_begin + t) * kK, n0, &sm.full[s]);
       if constexpr (SPLIT) {
-        tma_load_2d(sm.al[s], &map_al, t * kTcK, m0, &sm.full[s]);
-        tma_load_2d(sm.bl[s], &map_bl, t * kTcK, n0, &sm.full[s]);
+        tma_load_2d(sm.al[s], &map_al, (t_begin + t) * kTcK, m0, &sm.full[s]);
+        tma_load_2d(sm.bl[s], &map_bl, (t_begin + t) * kTcK, n0, &sm.full[s]);
       }
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr unsigned idesc = idesc_tf32(kTcM, kTcN);
+    constexpr unsigned idesc = BF ? idesc_bf16(kTcM, kTcN) : idesc_tf32(kTcM, kTcN);
     int issued = 0;
     for (int t = 0; t < ktiles; ++t) {
       const int s = t % kStages, r = t / kStages;
@@ -142,7 +160,10 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
       for (int k = 0; k < kTcK / 8; ++k) {  // K = 8 TF32 (32 bytes) per instruction
         const unsigned long long ad = smem_desc_sw128(sm.a[s]) + ((k * 32) >> 4);
         const unsigned long long bd = smem_desc_sw128(sm.b[s]) + ((k * 32) >> 4);
-        mma_tf32(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+        if constexpr (BF)
+          mma_bf16(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+        else
+          mma_tf32(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
         if constexpr (SPLIT) {
           const unsigned long long ald = smem_desc_sw128(sm.al[s]) + ((k * 32) >> 4);
           const unsigned long long bld = smem_desc_sw128(sm.bl[s]) + ((k * 32) >> 4);
@@ -262,18 +283,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D FP32 map over rows×cols (row stride ld elements), box kTcK × 128.
-static int make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld) {
+// 2-D map over rows×cols (row stride ld elements) with 128-byte rows per box:
+// FP32 (box 32 × 128) or BF16 (box 64 × 128).
+static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld,
+                    bool bf16 = false) {
   auto fn = encode_fn();
   if (!fn) {
     set_last_error("gemm_tf32: cuTensorMapEncodeTiled unavailable");
     return LXGB_CUDA_ERROR;
   }
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float))};
-  cuuint32_t box[2] = {(cuuint32_t)kTcK, 128u};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * (bf16 ? 2 : 4))};
+  cuuint32_t box[2] = {(cuuint32_t)(bf16 ? 2 * kTcK : kTcK), 128u};
   cuuint32_t estr[2] = {1u, 1u};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+  CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                  2, const_cast<void*>(base), dims, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -323,16 +347,16 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
   dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
   if (split) {
     const size_t smem = sizeof(TcSmem<kTcStagesSplit, true>) + 1024;
-    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<true>), (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<1>), (int)smem),
                   "gemm_tf32: set smem");
-    gemm_tf32_nt_kernel<true><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
-                                                             N, K, C, ldc, alpha, beta, err);
+    gemm_tf32_nt_kernel<1><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
+                                                          N, K, C, ldc, alpha, beta, err, 0, 0);
   } else {
     const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
-    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<false>), (int)smem),
+    LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<0>), (int)smem),
                   "gemm_tf32: set smem");
-    gemm_tf32_nt_kernel<false><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
-                                                              N, K, C, ldc, alpha, beta, err);
+    gemm_tf32_nt_kernel<0><<<grid, kTcThreads, smem, st>>>(ma, mb, mal, mbl, mc, use_tma_c, M,
+                                                          N, K, C, ldc, alpha, beta, err, 0, 0);
   }
   return check_launch("gemm_tf32");
 }
@@ -341,6 +365,81 @@ int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* 
                  float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
   return gemm_tf32_nt_split(M, N, K, A, nullptr, lda, B, nullptr, ldb, C, ldc, alpha, beta, err,
                             st);
+}
+
+// Split-K: C_s = A[:, K_s] B[:, K_s]ᵀ for s < splits, K_s the s-th range of
+// chunk elements (chunk a multiple of 32), C_s at C + s * M * ldc — one launch
+// (blockIdx.z = s) instead of one per range.  Pointer epilogue (rows past M
+// are not written).
+int gemm_tf32_nt_splitk(int M, int N, int K, const float* A, int64_t lda, const float* B,
+                        int64_t ldb, float* C, int64_t ldc, int chunk, int splits, int* err,
+                        cudaStream_t st) {
+  if (M <= 0 || N <= 0 || splits <= 0) return LXGB_SUCCESSFUL;
+  if ((chunk % kTcK) != 0 || chunk <= 0) return invalid("gemm_tf32 split-K: chunk not a multiple of 32");
+  CUtensorMap ma, mb;
+  int rc = make_map(&ma, A, M, K, lda);
+  if (rc) return rc;
+  rc = make_map(&mb, B, N, K, ldb);
+  if (rc) return rc;
+  dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM), (unsigned)splits);
+  const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<0>), (int)smem),
+                "gemm_tf32: set smem");
+  gemm_tf32_nt_kernel<0><<<grid, kTcThreads, smem, st>>>(ma, mb, ma, mb, ma, 0, M, N, K, C, ldc,
+                                                        1.0f, 0.0f, err, chunk / kTcK,
+                                                        (int64_t)M * ldc);
+  return check_launch("gemm_tf32 split-K");
+}
+
+// C = alpha A Bᵀ + beta C with BF16 operands (A m×k, B n×k, K-major, row
+// strides multiples of 8 elements, 16-byte aligned), FP32 C.
+int gemm_bf16_nt(int M, int N, int K, const void* A, int64_t lda, const void* B, int64_t ldb,
+                 float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return LXGB_SUCCESSFUL;
+  if (K == 0) {
+    const int64_t total = (int64_t)M * N;
+    scale_c_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(M, N, C, ldc, beta);
+    return check_launch("gemm_bf16 (k = 0)");
+  }
+  CUtensorMap ma, mb;
+  int rc = make_map(&ma, A, M, K, lda, true);
+  if (rc) return rc;
+  rc = make_map(&mb, B, N, K, ldb, true);
+  if (rc) return rc;
+  CUtensorMap mc = ma;
+  int use_tma_c = 0;
+  if ((((uintptr_t)C) & 15) == 0 && (ldc % 4) == 0 && make_map(&mc, C, M, N, ldc) == 0)
+    use_tma_c = 1;
+  else
+    cudaGetLastError();
+  dim3 grid((unsigned)((N + kTcN - 1) / kTcN), (unsigned)((M + kTcM - 1) / kTcM));
+  const size_t smem = sizeof(TcSmem<kTcStages, false>) + 1024;
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(gemm_tf32_nt_kernel<2>), (int)smem),
+                "gemm_bf16: set smem");
+  gemm_tf32_nt_kernel<2><<<grid, kTcThreads, smem, st>>>(ma, mb, ma, mb, mc, use_tma_c, M, N, K,
+                                                        C, ldc, alpha, beta, err, 0, 0);
+  return check_launch("gemm_bf16");
+}
+
+// dst (rows × cols, row stride ldd) = src rounded to BF16 (nearest even).
+__global__ void bf16_convert_kernel(int64_t rows, int64_t cols, const float* __restrict__ src,
+                                    int64_t lds, __nv_bfloat16* __restrict__ dst, int64_t ldd) {
+  const int64_t total = rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / cols, c = e % cols;
+    dst[r * ldd + c] = __float2bfloat16_rn(src[r * lds + c]);
+  }
+}
+
+int bf16_convert(int64_t rows, int64_t cols, const float* src, int64_t lds, void* dst, int64_t ldd,
+                 cudaStream_t st) {
+  const int64_t total = rows * cols;
+  if (total <= 0) return LXGB_SUCCESSFUL;
+  const int64_t blocks = (total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096;
+  bf16_convert_kernel<<<(unsigned)blocks, 256, 0, st>>>(rows, cols, src, lds,
+                                                        reinterpret_cast<__nv_bfloat16*>(dst), ldd);
+  return check_launch("bf16_convert");
 }
 
 // hi = x with the low 13 mantissa bits cleared (TF32-exact), lo = x - hi
@@ -403,4 +502,20 @@ extern "C" int lxgb_gemm_3xtf32_nt(int32_t m, int32_t n, int32_t k, const float*
                "gemm_3xtf32: lo parts must be 16-byte aligned");
   return gemm_tf32_nt_split(m, n, k, a, a_lo, lda, b, b_lo, ldb, c, ldc, alpha, beta, err,
                             as_stream(stream));
+}
+
+extern "C" int lxgb_gemm_bf16_nt(int32_t m, int32_t n, int32_t k, const void* a, int64_t lda,
+                                 const void* b, int64_t ldb, float* c, int64_t ldc, float alpha,
+                                 float beta, int32_t* err, void* stream) {
+  LXGB_REQUIRE(m >= 0 && n >= 0 && k >= 0, "gemm_bf16: negative size");
+  if (m == 0 || n == 0) return LXGB_SUCCESSFUL;
+  LXGB_REQUIRE(c && err && (k == 0 || (a && b)), "gemm_bf16: null pointer");
+  LXGB_REQUIRE(ldc >= n, "gemm_bf16: ldc < n");
+  if (k > 0) {
+    LXGB_REQUIRE(lda >= k && ldb >= k, "gemm_bf16: leading dimension too small");
+    LXGB_REQUIRE((lda % 8) == 0 && (ldb % 8) == 0, "gemm_bf16: lda and ldb must be multiples of 8");
+    LXGB_REQUIRE((((uintptr_t)a) & 15) == 0 && (((uintptr_t)b) & 15) == 0,
+                 "gemm_bf16: A and B must be 16-byte aligned");
+  }
+  return gemm_bf16_nt(m, n, k, a, lda, b, ldb, c, ldc, alpha, beta, err, as_stream(stream));
 }

@@ -18,6 +18,17 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
 // (ir.cu).
 int launch_inv_diag_lower(int n, int j0, int nb, const float* lu, float* w, int c_begin,
                           int c_end, float* xt, cudaStream_t st);
+// Split-K products C_s = A[:, K_s] B[:, K_s]ᵀ (K_s: splits ranges of chunk
+// elements, chunk % 32 == 0), C_s at C + s * M * ldc, in one launch.
+int gemm_tf32_nt_splitk(int M, int N, int K, const float* A, int64_t lda, const float* B,
+                        int64_t ldb, float* C, int64_t ldc, int chunk, int splits, int* err,
+                        cudaStream_t st);
+// BF16 operands (kind::f16, FP32 accumulation); A and B hold __nv_bfloat16.
+int gemm_bf16_nt(int M, int N, int K, const void* A, int64_t lda, const void* B, int64_t ldb,
+                 float* C, int64_t ldc, float alpha, float beta, int* err, cudaStream_t st);
+// dst = src rounded to BF16 (rows × cols; row strides in elements).
+int bf16_convert(int64_t rows, int64_t cols, const float* src, int64_t lds, void* dst, int64_t ldd,
+                 cudaStream_t st);
 // hi/lo split of a rows×cols block (row stride lds) into hi, lo (row stride ldd).
 int tf32_split(int64_t rows, int64_t cols, const float* src, int64_t lds, float* hi, float* lo,
                int64_t ldd, cudaStream_t st);

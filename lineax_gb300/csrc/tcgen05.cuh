@@ -63,6 +63,23 @@ __device__ __forceinline__ void mma_tf32(unsigned tmem_d, unsigned long long ade
       : "memory");
 }
 
+// Instruction descriptor, kind::f16 with BF16 A and B (format 1 in bits 7-9
+// and 10-12; both operands must have the same type), D = F32, both K-major.
+__host__ __device__ constexpr unsigned idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) |
+         ((unsigned)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(unsigned tmem_d, unsigned long long adesc,
+                                         unsigned long long bdesc, unsigned idesc, int accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(unsigned long long* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(

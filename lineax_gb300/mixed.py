@@ -38,12 +38,16 @@ class LU32:
     info: torch.Tensor  # device int32
 
 
-PRECISIONS = {"tf32": 0, "3xtf32": 1}
+PRECISIONS = {"tf32": 0, "3xtf32": 1, "bf16": 2}
+# Factor precisions from the cheapest to the most accurate: a solve that stalls
+# with one factor moves to the next before it falls back to FP64.
+LADDER = ("bf16", "tf32", "3xtf32")
 
 
 def lu_factor_tf32(a: torch.Tensor, precision: str = "tf32") -> LU32:
     """FP32 LU with partial pivoting and tensor-core trailing updates:
-    precision "tf32" (one TF32 product) or "3xtf32" (FP32-level accuracy)."""
+    precision "bf16" (BF16 products, FP32 accumulation), "tf32" (one TF32
+    product) or "3xtf32" (FP32-level accuracy)."""
     a64 = as_device_f64(a)
     n = a64.shape[0]
     if a64.shape != (n, n):
@@ -117,7 +121,7 @@ def lu_inverse(factor: LU32, precision: str = "3xtf32") -> InverseLU32:
     uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
     perm = torch.empty(n, dtype=torch.int32, device=dev)
     err = torch.zeros(1, dtype=torch.int32, device=dev)
-    prec = PRECISIONS[precision]
+    prec = min(PRECISIONS[precision], 1)  # a BF16 factor's inverses use TF32 updates
     wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, prec))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(lu), _ffi.ptr(factor.piv), _ffi.ptr(linv),
@@ -265,6 +269,7 @@ class IRResult:
     converged: bool
     fallback: bool = False   # solved by the FP64 LU after GMRES-IR stalled
     inverse: InverseLU32 | None = None  # the triangular inverses, when they were formed
+    tiers: list = dataclasses.field(default_factory=list)  # (factor, outer, converged) tried
 
 
 def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol: float = 1e-6,
@@ -272,7 +277,8 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
              inner_max_steps: int | None = None, factor: LU32 | None = None,
              inverse: InverseLU32 | None = None, split: SplitMatrix | None = None,
              precision: str = "3xtf32", arith: str = "df", fallback: bool = False,
-             qr: "SquareQR32 | None" = None, device_loop: bool = True) -> IRResult:
+             qr: "SquareQR32 | None" = None, device_loop: bool = True,
+             escalate: bool = False, stop_on_stall: bool | None = None) -> IRResult:
     """GMRES-based iterative refinement for A X = B (B: (k, n) FP64).
 
     Each refinement step solves A d = r / ||r||_inf with GMRES (lineax
@@ -300,6 +306,12 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     Householder QR solve: lineax's QR solver (lineax/_solver/qr.py:55-94) on
     a square operator, recovered to FP64 accuracy the same way.
 
+    escalate=True (LU preconditioner, arith "auto"): a solve that stalls with
+    the given factor precision is repeated with the next one of LADDER (BF16 →
+    TF32 → 3xTF32) before the FP64 fallback; IRResult.tiers lists what was
+    tried.  stop_on_stall (default: fallback) ends the loop at the first stall
+    of the GMRES tier.
+
     device_loop (arith "auto" with the LU preconditioner) runs the whole
     refinement loop as one call of lxgb_gmres_ir_run — the same kernels in the
     same order, with the loop decisions taken on the device — and returns to
@@ -310,6 +322,31 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
         b64 = b64.reshape(1, -1)
     b64 = b64.contiguous()
     k, n = b64.shape
+    if stop_on_stall is None:
+        stop_on_stall = fallback
+    if escalate and qr is None and arith == "auto" and precision in LADDER:
+        if split is None:
+            split = split_matrix(a64)
+        tried, res = [], None
+        for prec in LADDER[LADDER.index(precision):]:
+            f = factor if prec == precision and factor is not None else lu_factor_tf32(a64, prec)
+            inv = inverse if prec == precision else None
+            res = gmres_ir(a64, b64, tol=tol, inner_rtol=inner_rtol, restart=restart,
+                           stagnation_iters=stagnation_iters, max_outer=max_outer,
+                           inner_max_steps=inner_max_steps, factor=f, inverse=inv, split=split,
+                           precision=prec, arith=arith, fallback=False, device_loop=device_loop,
+                           stop_on_stall=True)
+            tried.append((prec, res.outer, res.converged))
+            if res.converged:
+                res.tiers = tried
+                return res
+        if fallback:
+            outer_op = SplitMatrixOperator(split, "df")
+            res = _fp64_fallback(a64, b64, outer_op, float(norm_inf(a64).item()),
+                                 _kmax(b64).cpu(), tol, res.outer, res.inner_steps)
+            tried.append(("fp64", 1, res.converged))
+        res.tiers = tried
+        return res
     if factor is None and qr is None:
         factor = lu_factor_tf32(a64, precision)
     if split is None:
@@ -319,7 +356,8 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
         if inverse is None:
             inverse = lu_inverse(factor, precision)
         return _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart,
-                                stagnation_iters, max_outer, inner_max_steps, fallback)
+                                stagnation_iters, max_outer, inner_max_steps, fallback,
+                                stop_on_stall)
     tiers = ["ir", "df"] if arith == "auto" else [arith]
     tier = 0
     made = {"inverse": inverse}
@@ -367,7 +405,9 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
         if stalled and tier + 1 < len(tiers):
             tier += 1
             inner_op, pre = inner(tier)
-        elif fallback and stalled:
+        elif stop_on_stall and stalled:
+            if not fallback:
+                break
             return _fp64_fallback(a64, b64, outer_op, anorm, bnorm, tol, it, inner_steps,
                                   qr is not None)
     if fallback and not converged:
@@ -377,7 +417,7 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
 
 
 def _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart, stagnation_iters,
-                     max_outer, inner_max_steps, fallback) -> IRResult:
+                     max_outer, inner_max_steps, fallback, stop_on_stall) -> IRResult:
     """gmres_ir's "auto" loop as one lxgb_gmres_ir_run call."""
     import ctypes
 
@@ -398,7 +438,7 @@ def _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart, stagnat
     inner_steps = 5 if inner_max_steps is None else int(inner_max_steps)
     _ffi.call("lxgb_gmres_ir_run", k, n, ctypes.addressof(op), ctypes.addressof(pre),
               _ffi.ptr(b64), _ffi.ptr(x), _ffi.ptr(anorm), float(tol), float(inner_rtol),
-              int(max_outer), R, inner_steps, int(stagnation_iters), int(bool(fallback)),
+              int(max_outer), R, inner_steps, int(stagnation_iters), int(bool(stop_on_stall)),
               _ffi.ptr(berr), _ffi.ptr(status), _ffi.ptr(work), work.numel() * 8,
               _ffi.stream_handle(dev))
     outer, reached_gmres, code = status.cpu().tolist()

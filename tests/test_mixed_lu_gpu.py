@@ -205,3 +205,40 @@ def test_gmres_ir_single_call_equals_host_loop(dev, n, cond, precision, max_oute
     assert host.outer == devl.outer and host.converged == devl.converged
     assert host.berr == devl.berr
     assert (max(host.inner_steps) > 0) == (max(devl.inner_steps) > 0)
+
+
+@pytest.mark.parametrize("n", [256, 1024, 2048])
+def test_bf16_lu_factorisation_residual(dev, n):
+    """BF16 tensor-core updates (8-bit significands, FP32 accumulation): the
+    factor reproduces P A to a small multiple of u = 2^-8 (the TF32 test's
+    bound, 3e-2, is about 60 of its u = 2^-11; measured here: 23 u at n = 2048)."""
+    a = conditioned(n, 1e2, n + 3)
+    f = mixed.lu_factor_tf32(torch.tensor(a, device=dev), "bf16")
+    assert int(f.info) == 0
+    lu = f.lu.double().cpu().numpy()
+    piv = f.piv.cpu().numpy()
+    l = np.tril(lu, -1) + np.eye(n)
+    u = np.triu(lu)
+    pa = a.copy()
+    for k in range(n):
+        pa[[k, piv[k]]] = pa[[piv[k], k]]
+    rel = np.linalg.norm(pa - l @ u) / np.linalg.norm(a)
+    assert rel < 64 * 2.0 ** -8, rel
+
+
+@pytest.mark.parametrize("cond", [1e2, 1e6])
+def test_gmres_ir_precision_ladder(dev, cond):
+    """A factor that stalls moves up the ladder BF16 -> TF32 -> 3xTF32 before
+    any FP64 fallback: at cond 1e2 and 1e6 the solve ends on a low-precision
+    factor, at backward error <= 1e-12, and reports the tiers it tried."""
+    n = 1024
+    a = conditioned(n, cond, 77)
+    b = np.random.default_rng(3).standard_normal((4, n))
+    res = mixed.gmres_ir(torch.tensor(a, device=dev), torch.tensor(b, device=dev), tol=1e-12,
+                         restart=8, inner_max_steps=5, precision="bf16", arith="auto",
+                         fallback=True, escalate=True)
+    assert res.converged and not res.fallback, res.tiers
+    assert res.tiers[0][0] == "bf16" and res.tiers[-1][2]
+    x = res.x.cpu().numpy()
+    be = dense.backward_errors_exact(a, x, b)
+    assert (be <= 1e-12 * (1 + 1e-4)).all(), be

@@ -86,3 +86,31 @@ def test_tf32_gemm_epilogue_layouts(dev, layout):
         else:
             mask[1:, 1:n + 1] = False
         assert torch.equal(big[mask], outside[mask])
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (128, 128, 16), (256, 384, 200),
+                                   (1000, 700, 64), (130, 260, 96), (512, 512, 512)])
+def test_bf16_gemm_matches_reference(dev, m, n, k):
+    """lxgb_gemm_bf16_nt (tcgen05 kind::f16, BF16 operands, FP32 accumulation):
+    products of BF16 values are exact in FP32, so against the product of the
+    BF16-rounded operands the error is the FP32 accumulation's, k 2^-24."""
+    from lineax_gb300 import _ffi
+
+    g = torch.Generator(device=dev).manual_seed(m * 17 + n * 3 + k)
+    a = torch.randn(m, k, device=dev, generator=g).to(torch.bfloat16)
+    b = torch.randn(n, k, device=dev, generator=g).to(torch.bfloat16)
+    ka = (k + 7) // 8 * 8  # row strides: multiples of 8 elements (16 bytes)
+    ap = torch.zeros(m, ka, dtype=torch.bfloat16, device=dev)
+    bp = torch.zeros(n, ka, dtype=torch.bfloat16, device=dev)
+    ap[:, :k] = a
+    bp[:, :k] = b
+    c = torch.randn(m, n, device=dev, generator=g)
+    c0 = c.clone()
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    _ffi.call("lxgb_gemm_bf16_nt", m, n, k, _ffi.ptr(ap), ka, _ffi.ptr(bp), ka, _ffi.ptr(c), n,
+              -1.0, 1.0, _ffi.ptr(err), _ffi.stream_handle(dev))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    r = c0.double() - a.double() @ b.double().T
+    scale = (a.double().abs() @ b.double().abs().T) + c0.double().abs()
+    assert float(((c.double() - r).abs() / scale).max()) <= (k + 2) * 2.0 ** -23
