@@ -387,6 +387,7 @@ def run_gpu(args):
             "parallelism": f"replicas x{world}",
             "launch": "one persistent posv_mixed_kernel launch per step, replayed from a "
                       "captured CUDA graph",
+            "trailing_update": "tcgen05 TF32 split" if args.tensor_core_update else "FP32 cores",
         },
         "latency_ms": {"p50": _pct(per_step, 50), "p99": _pct(per_step, 99)},
         "correct": {"all_berr_le_tol": ok, "max_berr": float(berr.max()),
@@ -988,9 +989,10 @@ def run_serve(args):
 
 def run_peaks(args):
     """Arithmetic reference points on this GPU: library GEMMs (torch.matmul,
-    FP64 / FP32 / TF32, a sanity line) and this library's tcgen05 TF32 and
-    3xTF32 GEMM on the same square shape and on the rank-64 update shape of
-    the LU factorisations.  Best of 5 CUDA-event timings after 2 warm-ups."""
+    FP64 / FP32 / TF32 / BF16, a sanity line) and this library's tcgen05 TF32,
+    3xTF32 and BF16 GEMMs (persistent kernel, and the one-tile-per-CTA kernel
+    beside it) on the same square shape and on the rank-64 update shape of the
+    LU factorisations.  Best of 5 CUDA-event timings after 2 warm-ups."""
     import torch
 
     from lineax_gb300 import _blas
@@ -1028,14 +1030,35 @@ def run_peaks(args):
         out["torch_tf32_tflops"] = best(lambda: a32 @ b32, fl)
         torch.backends.cuda.matmul.allow_tf32 = False
         del a64, b64
-    out["lxgb_tf32_tflops"] = best(lambda: _blas.gemm_tf32_nt(a32, b32, c32), fl)
-    out["lxgb_3xtf32_tflops"] = best(lambda: _blas.gemm_3xtf32_nt(a32, b32, c32), fl)
+    from lineax_gb300 import _ffi
+
+    a16 = a32.to(torch.bfloat16)
+    b16 = b32.to(torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def bf16_gemm(a, b, c, alpha=1.0, beta=0.0):
+        _ffi.call("lxgb_gemm_bf16_nt", a.shape[0], b.shape[0], a.shape[1], _ffi.ptr(a),
+                  a.stride(0), _ffi.ptr(b), b.stride(0), _ffi.ptr(c), c.stride(0), alpha, beta,
+                  _ffi.ptr(err), _ffi.stream_handle(dev))
+
+    if not args.peaks_ours_only:
+        out["torch_bf16_tflops"] = best(lambda: a16 @ b16.T, fl)
     # the LU trailing update: C (n×n) -= A (n×64) Bᵀ (n×64), C read and written
     a_k = a32[:, :64].contiguous()
     b_k = b32[:, :64].contiguous()
-    t = best(lambda: _blas.gemm_tf32_nt(a_k, b_k, c32, alpha=-1.0, beta=1.0), 2.0 * n * n * 64)
-    out["lxgb_tf32_rank64_tflops"] = t
-    out["lxgb_tf32_rank64_gbs"] = t * 1e12 / (2.0 * n * n * 64) * (8.0 * n * n) / 1e9
+    for tag, on in (("", 1), ("_tile", 0)):
+        # "" = the persistent kernel (default), "_tile" = one CTA per 128×128 tile
+        _ffi.call("lxgb_gemm_set_persistent", on)
+        out[f"lxgb_tf32{tag}_tflops"] = best(lambda: _blas.gemm_tf32_nt(a32, b32, c32), fl)
+        out[f"lxgb_3xtf32{tag}_tflops"] = best(lambda: _blas.gemm_3xtf32_nt(a32, b32, c32), fl)
+        out[f"lxgb_bf16{tag}_tflops"] = best(lambda: bf16_gemm(a16, b16, c32), fl)
+        t = best(lambda: _blas.gemm_tf32_nt(a_k, b_k, c32, alpha=-1.0, beta=1.0),
+                 2.0 * n * n * 64)
+        out[f"lxgb_tf32{tag}_rank64_tflops"] = t
+        out[f"lxgb_tf32{tag}_rank64_gbs"] = t * 1e12 / (2.0 * n * n * 64) * (8.0 * n * n) / 1e9
+    _ffi.call("lxgb_gemm_set_persistent", 1)
+    torch.cuda.synchronize()
+    out["pipeline_timeouts"] = int(err.item())
     print(json.dumps(out), flush=True)
 
 
@@ -1049,6 +1072,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline measurement")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving suite in the default line")
+    p.add_argument("--tensor-core-update", action="store_true",
+                   help="ragged factor: trailing updates on the tensor cores (TF32 split)")
     p.add_argument("--systems", type=int, default=COUNT,
                    help="systems per GPU (smaller values are for profiling runs only)")
     p.add_argument("--workload", default="ragged_cholesky",
@@ -1082,6 +1107,9 @@ def main():
                    help="time the plain FP64 LU at every condition number (gmres_ir)")
     args = p.parse_args()
     COUNT = args.systems
+    if args.tensor_core_update:
+        from lineax_gb300 import _ffi
+        _ffi.call("lxgb_posv_mixed_set_tensor_cores", 1)
     modes = {"gmres_ir": run_gmres_ir, "lu_batch": run_lu_batch, "qr_ls": run_qr_ls,
              "cg_poisson": run_cg_poisson, "serve": run_serve, "peaks": run_peaks,
              "cholesky_large": run_cholesky_large}

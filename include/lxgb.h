@@ -505,6 +505,14 @@ int lxgb_gemm_bf16_nt(int32_t m, int32_t n, int32_t k, const void* a, int64_t ld
                       const void* b, int64_t ldb, float* c, int64_t ldc, float alpha,
                       float beta, int32_t* err, void* stream);
 
+/* Kernel choice of the three GEMMs above (a tuning switch, process-wide;
+ * results are the same up to the order of the FP32 accumulation): 1 (the
+ * default) runs them as one persistent launch of one CTA per SM with two
+ * tensor-memory accumulators (128×256 tiles; 128×128 for 3xTF32), so the
+ * epilogue of one tile overlaps the products of the next — used whenever C is
+ * 16-byte aligned with ldc a multiple of 4; 0 runs one CTA per 128×128 tile. */
+int lxgb_gemm_set_persistent(int32_t on);
+
 /* Mixed-precision LU for GMRES-IR: P A = L U in FP32 with partial pivoting
  * (first row of max |a|), 64-column panels, trailing updates on the tcgen05
  * tensor cores with FP32 accumulation: precision 0 = TF32 products, 1 =

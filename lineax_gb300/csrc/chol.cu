@@ -156,21 +156,23 @@ struct MxSmem {
 };
 
 
-// Split W FP64 values with one warp vote (see split_f64).
+// Split W FP64 values, given as their two 32-bit words (x = low, y = high),
+// with one warp vote (see split_f64).  Only 32-bit integer operations run on
+// the common path.
 template <int W>
-__device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], float (&lo)[W]) {
+__device__ __forceinline__ void splitw(const uint2 (&a)[W], float (&hi)[W], float (&lo)[W]) {
   bool slow = false;
 #pragma unroll
   for (int u = 0; u < W; ++u) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(a[u]);
-    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-    const unsigned mh = (unsigned)(b >> 29) & 0x7FFFFFu;
-    const unsigned rem = (unsigned)b & 0x1FFFFFFFu;
+    const unsigned wl = a[u].x, wh = a[u].y;
+    const unsigned e = (wh >> 20) & 0x7FFu;
+    const unsigned sign = wh & 0x80000000u;
+    const unsigned mh = ((wh & 0xFFFFFu) << 3) | (wl >> 29);
+    const unsigned rem = wl & 0x1FFFFFFFu;
     const int sh = __clz(rem | 1u) - 8;
     const unsigned m = (sh >= 0) ? (rem << sh) : (rem >> (-sh));
     const int ex = (int)e - 1052 - sh + 127;
-    const bool zero = (b << 1) == 0ull;
+    const bool zero = ((wh << 1) | wl) == 0u;
     hi[u] = zero ? __uint_as_float(sign) : __uint_as_float(sign | (((e - 1023u + 127u) & 0xFFu) << 23) | mh);
     lo[u] = (rem == 0u) ? 0.0f : __uint_as_float(sign | (((unsigned)ex & 0xFFu) << 23) | (m & 0x7FFFFFu));
     slow |= !zero && ((e < 949u) || (e > 1150u));
@@ -178,10 +180,12 @@ __device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], flo
   if (__any_sync(__activemask(), slow)) {
 #pragma unroll
     for (int u = 0; u < W; ++u) {
-      const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a[u]) >> 52) & 0x7FFu;
-      if (a[u] != 0.0 && ((e < 949u) || (e > 1150u))) {
-        hi[u] = __double2float_rz(a[u]);
-        lo[u] = __double2float_rn(a[u] - (double)hi[u]);
+      const unsigned wl = a[u].x, wh = a[u].y;
+      const unsigned e = (wh >> 20) & 0x7FFu;
+      if (((wh << 1) | wl) != 0u && ((e < 949u) || (e > 1150u))) {
+        const double d = __hiloint2double((int)wh, (int)wl);
+        hi[u] = __double2float_rz(d);
+        lo[u] = __double2float_rn(d - (double)hi[u]);
       }
     }
   }
@@ -195,21 +199,21 @@ __device__ __forceinline__ void splitw(const double (&a)[W], float (&hi)[W], flo
 __device__ __forceinline__ void mx_copy_upper(const double* __restrict__ A, int n, float* F,
                                               int64_t ld) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  auto load = [&](int r, int j0, double (&v)[8]) {
-    const double* arow = A + (int64_t)r * n;
+  auto load = [&](int r, int j0, uint2 (&v)[8]) {
+    const uint2* arow = reinterpret_cast<const uint2*>(A + (int64_t)r * n);
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int j = j0 + lane + 32 * u;
-      v[u] = (r < n && j < n) ? arow[j] : 0.0;
+      v[u] = (r < n && j < n) ? arow[j] : make_uint2(0u, 0u);
     }
   };
   int i = warp, j0 = warp;
-  double v[8];
+  uint2 v[8];
   load(i, j0, v);
   while (i < n) {
     int ni = i, nj = j0 + 256;
     if (nj >= n) { ni = i + nw; nj = ni; }
-    double vn[8];
+    uint2 vn[8];
     load(ni, nj, vn);
     float hi[8], lo[8];
     splitw<8>(v, hi, lo);
@@ -797,15 +801,15 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
   // (and b of the next row) are issued before the current chunk is used, so
   // the DRAM latency of A overlaps the arithmetic.
   const int nch = (n + 255) >> 8;
-  auto load_chunk = [&](int r, int ch, double (&v)[8]) {
-    const double* rowp = A + (int64_t)r * n;
+  auto load_chunk = [&](int r, int ch, uint2 (&v)[8]) {
+    const uint2* rowp = reinterpret_cast<const uint2*>(A + (int64_t)r * n);
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int j = (ch << 8) + lane + 32 * u;
-      v[u] = (r < n && j < n) ? rowp[j] : 0.0;
+      v[u] = (r < n && j < n) ? rowp[j] : make_uint2(0u, 0u);
     }
   };
-  double av[8];
+  uint2 av[8];
   load_chunk(warp, 0, av);
   double bnext = (warp < n && cl < nc) ? B[(int64_t)cl * n + warp] : 0.0;
   for (int i = warp; i < n; i += nw) {
@@ -816,7 +820,7 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
     const double bval = bnext;
     for (int ch = 0; ch < nch; ++ch) {
       const int j0 = ch << 8;
-      double an[8];
+      uint2 an[8];
       if (ch + 1 < nch) {
         load_chunk(i, ch + 1, an);
       } else {

@@ -269,6 +269,310 @@ gemm_tf32_nt_kernel(const __grid_constant__ CUtensorMap map_a,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised form: one CTA per SM walks the output tiles
+// (BN = 256 columns for TF32 and BF16, 128 for 3xTF32) with two tensor-memory
+// accumulators, so the epilogue of tile i overlaps the MMAs of tile i+1.
+//   warp 0 lane 0   TMA producer: A and B stages into a kPS-deep ring;
+//   warp 1          allocates tensor memory; lane 0 issues tcgen05.mma into
+//                   accumulator (tile & 1) once the epilogue has emptied it;
+//   warps 2..5      epilogue: warp w reads TMEM lanes 32 (w % 4) ..+31 (rows
+//                   of the tile), 32 columns at a time; the old C chunk
+//                   (32 × 32) arrives by TMA one chunk ahead into a private
+//                   double buffer, is updated in place and leaves by TMA.
+// Tile order: groups of 8 row blocks, column blocks inside a group, so the
+// CTAs running at the same time share A rows and B columns in L2.
+// ---------------------------------------------------------------------------
+constexpr int kPThreads = 192;
+constexpr int kPEpiChunk = 32 * 32 * 4;  // one 32-row × 32-column FP32 C chunk
+
+template <int MODE, int S_, int CB_>
+struct PCfg {
+  static constexpr bool SPLIT = MODE == 1;
+  static constexpr int BN = SPLIT ? 128 : 256;
+  static constexpr int S = S_;                       // operand stages
+  static constexpr int CB = CB_;                     // C staging buffers per epilogue warp
+  static constexpr int A_BYTES = kTcM * 128;         // 128 rows of 128 bytes
+  static constexpr int B_BYTES = BN * 128;
+  static constexpr int STAGE_BYTES = (A_BYTES + B_BYTES) * (SPLIT ? 2 : 1);
+  static constexpr int OFF_B = S * A_BYTES;
+  static constexpr int OFF_AL = OFF_B + S * B_BYTES;
+  static constexpr int OFF_BL = OFF_AL + (SPLIT ? S * A_BYTES : 0);
+  static constexpr int OFF_C = OFF_BL + (SPLIT ? S * B_BYTES : 0);
+  static constexpr int OFF_BAR = OFF_C + 4 * CB * kPEpiChunk;
+  // full[S], empty[S], tfull[2], tempty[2], cbar[4][CB], done, then tmem base and abort
+  static constexpr int BAR_COUNT = 2 * S + 4 + 4 * CB + 1;
+  static constexpr int BYTES = OFF_BAR + BAR_COUNT * 8 + 16;
+  static constexpr int SMEM = BYTES + 1024;          // slack to align the base to 1 KB
+  static constexpr unsigned TMEM_COLS = 2 * BN;
+};
+// Long K: four operand stages keep the tensor pipe fed; short K (the rank-64
+// updates of the factorisations, one or two stages per tile): two stages and
+// six C buffers per warp, so that five chunks of old C (80 KB per SM) are in
+// flight while the epilogue streams C through HBM.
+using PCfgTf32 = PCfg<0, 4, 2>;
+using PCfgTf32ShortK = PCfg<0, 2, 6>;
+using PCfgSplit = PCfg<1, 3, 2>;
+using PCfgBf16 = PCfg<2, 4, 2>;
+using PCfgBf16ShortK = PCfg<2, 2, 6>;
+static_assert(PCfgTf32::SMEM <= 232448 && PCfgTf32ShortK::SMEM <= 232448 &&
+                  PCfgSplit::SMEM <= 232448 && PCfgBf16::SMEM <= 232448 &&
+                  PCfgBf16ShortK::SMEM <= 232448,
+              "persistent GEMM exceeds shared memory");
+
+__device__ __forceinline__ void tile_coords(int tile, int n_mblk, int n_nblk, int& mb, int& nb) {
+  constexpr int G = 8;
+  const int per_group = G * n_nblk;
+  const int group = tile / per_group;
+  const int first = group * G;
+  const int gsize = min(n_mblk - first, G);
+  const int in = tile - group * per_group;
+  mb = first + in % gsize;
+  nb = in / gsize;
+}
+
+template <int MODE, class Cfg>
+__global__ void __launch_bounds__(kPThreads, 1)
+gemm_nt_persistent_kernel(const __grid_constant__ CUtensorMap map_a,
+                          const __grid_constant__ CUtensorMap map_b,
+                          const __grid_constant__ CUtensorMap map_al,
+                          const __grid_constant__ CUtensorMap map_bl,
+                          const __grid_constant__ CUtensorMap map_c, int M, int N, int K,
+                          float alpha, float beta, int* err) {
+  constexpr bool SPLIT = Cfg::SPLIT;
+  constexpr bool BF = MODE == 2;
+  constexpr int BN = Cfg::BN, S = Cfg::S;
+  constexpr int kK = BF ? 2 * kTcK : kTcK;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(base + Cfg::OFF_BAR);
+  unsigned long long* full = bars;
+  unsigned long long* empty = bars + S;
+  unsigned long long* tfull = bars + 2 * S;
+  unsigned long long* tempty = bars + 2 * S + 2;
+  constexpr int CB = Cfg::CB;
+  unsigned long long* cbar = bars + 2 * S + 4;   // [4][CB]
+  unsigned long long* done = bars + 2 * S + 4 + 4 * CB;
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + Cfg::BAR_COUNT);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_mblk = (M + kTcM - 1) / kTcM, n_nblk = (N + BN - 1) / BN;
+  const int tiles = n_mblk * n_nblk;
+  const int ktiles = (K + kK - 1) / kK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < Cfg::BAR_COUNT; ++i) mbar_init(&bars[i], 1);
+    mbar_init(&tempty[0], 4);
+    mbar_init(&tempty[1], 4);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)), "r"(Cfg::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+  volatile int* vabort = abort_flag;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer ----------------
+      int it = 0;
+      for (int tile = blockIdx.x; tile < tiles && !*vabort; tile += gridDim.x) {
+        int mb, nb;
+        tile_coords(tile, n_mblk, n_nblk, mb, nb);
+        for (int t = 0; t < ktiles; ++t, ++it) {
+          const int s = it % S, r = it / S;
+          if (!mbar_wait(&empty[s], (r & 1) ^ 1)) { atomicExch(abort_flag, 1); break; }
+          if (*vabort) break;
+          mbar_expect_tx(&full[s], Cfg::STAGE_BYTES);
+          tma_load_2d(base + s * Cfg::A_BYTES, &map_a, t * kK, mb * kTcM, &full[s]);
+          tma_load_2d(base + Cfg::OFF_B + s * Cfg::B_BYTES, &map_b, t * kK, nb * BN, &full[s]);
+          if constexpr (SPLIT) {
+            tma_load_2d(base + Cfg::OFF_AL + s * Cfg::A_BYTES, &map_al, t * kK, mb * kTcM,
+                        &full[s]);
+            tma_load_2d(base + Cfg::OFF_BL + s * Cfg::B_BYTES, &map_bl, t * kK, nb * BN,
+                        &full[s]);
+          }
+        }
+      }
+      // the last S stages issued have landed before shared memory is released
+      for (int j = (it > S ? it - S : 0); j < it; ++j)
+        if (!mbar_wait(&full[j % S], (j / S) & 1)) atomicExch(abort_flag, 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr unsigned idesc = BF ? idesc_bf16(kTcM, BN) : idesc_tf32(kTcM, BN);
+      int it = 0, tc = 0;
+      for (int tile = blockIdx.x; tile < tiles && !*vabort; tile += gridDim.x, ++tc) {
+        const int buf = tc & 1, use = tc >> 1;
+        if (!mbar_wait(&tempty[buf], (use & 1) ^ 1)) { atomicExch(abort_flag, 1); break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const unsigned d = tmem + (unsigned)(buf * BN);
+        bool ok = true;
+        for (int t = 0; t < ktiles; ++t, ++it) {
+          const int s = it % S, r = it / S;
+          if (!mbar_wait(&full[s], r & 1)) { atomicExch(abort_flag, 1); ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const unsigned char* sa = base + s * Cfg::A_BYTES;
+          const unsigned char* sb = base + Cfg::OFF_B + s * Cfg::B_BYTES;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {  // 32 bytes of K per instruction
+            const unsigned long long ad = smem_desc_sw128(sa) + (unsigned long long)(2 * k);
+            const unsigned long long bd = smem_desc_sw128(sb) + (unsigned long long)(2 * k);
+            if constexpr (BF)
+              mma_bf16(d, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+            else
+              mma_tf32(d, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+            if constexpr (SPLIT) {
+              const unsigned long long ald =
+                  smem_desc_sw128(base + Cfg::OFF_AL + s * Cfg::A_BYTES) + (unsigned long long)(2 * k);
+              const unsigned long long bld =
+                  smem_desc_sw128(base + Cfg::OFF_BL + s * Cfg::B_BYTES) + (unsigned long long)(2 * k);
+              mma_tf32(d, ad, bld, idesc, 1);
+              mma_tf32(d, ald, bd, idesc, 1);
+            }
+          }
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&tfull[buf]);
+      }
+      // every MMA issued has completed before tensor memory is freed
+      mma_commit(done);
+      if (!mbar_wait(done, 0)) atomicExch(abort_flag, 1);
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int ew = warp - 2, q = warp & 3;
+    unsigned char* cst = base + Cfg::OFF_C + ew * CB * kPEpiChunk;
+    unsigned long long* cb = cbar + CB * ew;
+    constexpr int kChunks = BN / 32;
+    static_assert(CB <= kChunks + 1, "prefetch reaches past the next tile");
+    const bool load_c = beta != 0.0f;
+    unsigned cphase[CB];   // next phase to wait for, per staging buffer
+    bool pending[CB];      // lane 0: a load into the buffer is in flight
+#pragma unroll
+    for (int b2 = 0; b2 < CB; ++b2) { cphase[b2] = 0u; pending[b2] = false; }
+    // chunk d places after (tile, c): at most one tile further
+    auto chunk_at = [&](int tile, int c, int d, int& x, int& y) -> bool {
+      c += d;
+      if (c >= kChunks) { c -= kChunks; tile += gridDim.x; }
+      if (tile >= tiles) return false;
+      int mb, nb;
+      tile_coords(tile, n_mblk, n_nblk, mb, nb);
+      x = nb * BN + 32 * c;
+      y = mb * kTcM + 32 * q;
+      return x < N && y < M;   // chunks wholly outside C are skipped
+    };
+    // The warp's chunks (tile, c) are numbered g = 0, 1, ...; chunk g uses
+    // staging buffer g % CB, and chunk g + CB - 1's old C is requested before
+    // chunk g is processed.
+    if (load_c && blockIdx.x < tiles && lane == 0) {
+      for (int d = 0; d < CB - 1; ++d) {
+        int x, y;
+        if (chunk_at(blockIdx.x, 0, d, x, y)) {
+          mbar_expect_tx(&cb[d], kPEpiChunk);
+          tma_load_2d(cst + d * kPEpiChunk, &map_c, x, y, &cb[d]);
+          pending[d] = true;
+        }
+      }
+    }
+    bool ok = true;
+    int g = 0, tc = 0, last_store_buf = -1;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++tc) {
+      const int buf = tc & 1, use = tc >> 1;
+      ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], use & 1));
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int c = 0; c < kChunks; ++c, ++g) {
+        const int sbuf = g % CB;
+        unsigned char* cur = cst + sbuf * kPEpiChunk;
+        int cx = 0, cy = 0;
+        const bool live = chunk_at(tile, c, 0, cx, cy);
+        if (load_c && lane == 0) {
+          const int nbuf = (g + CB - 1) % CB;   // last used by chunk g - 1
+          int x, y;
+          if (chunk_at(tile, c, CB - 1, x, y)) {
+            // every store issued so far has finished reading its buffer
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            mbar_expect_tx(&cb[nbuf], kPEpiChunk);
+            tma_load_2d(cst + nbuf * kPEpiChunk, &map_c, x, y, &cb[nbuf]);
+            pending[nbuf] = true;
+          }
+        }
+        if (!live) continue;
+        if (load_c) {
+          ok = __all_sync(0xffffffffu, mbar_wait(&cb[sbuf], cphase[sbuf]));
+          if (ok) { cphase[sbuf] ^= 1u; pending[sbuf] = false; }
+        } else if (lane == 0) {
+          // the last store from this buffer has finished reading it: it is the
+          // newest bulk group or an older one
+          if (last_store_buf == sbuf)
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          else
+            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        }
+        __syncwarp();
+        float v[32];
+        tmem_ld32(tmem + ((unsigned)(32 * q) << 16) + (unsigned)(buf * BN + 32 * c), v);
+        if (!ok) break;
+        char* rowp = reinterpret_cast<char*>(cur) + lane * 128;
+#pragma unroll
+        for (int gq = 0; gq < 8; ++gq) {
+          float4* p4 = reinterpret_cast<float4*>(rowp + ((gq ^ (lane & 7)) << 4));
+          float4 o = load_c ? *p4 : make_float4(0.f, 0.f, 0.f, 0.f);
+          o.x = fmaf(alpha, v[4 * gq + 0], load_c ? beta * o.x : 0.0f);
+          o.y = fmaf(alpha, v[4 * gq + 1], load_c ? beta * o.y : 0.0f);
+          o.z = fmaf(alpha, v[4 * gq + 2], load_c ? beta * o.z : 0.0f);
+          o.w = fmaf(alpha, v[4 * gq + 3], load_c ? beta * o.w : 0.0f);
+          *p4 = o;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          tma_store_2d(&map_c, cx, cy, cur);
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          last_store_buf = sbuf;
+        }
+      }
+      if (!ok) break;
+      // this warp's reads of accumulator buf are complete (tcgen05.ld waited)
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[buf]))
+                     : "memory");
+      if (__any_sync(0xffffffffu, *vabort != 0)) break;
+    }
+    if (!ok) atomicExch(abort_flag, 1);
+    if (lane == 0) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      // a requested chunk that was never consumed lands before shared memory is released
+#pragma unroll
+      for (int b2 = 0; b2 < CB; ++b2)
+        if (pending[b2]) mbar_wait(&cb[b2], cphase[b2]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (*vabort && threadIdx.x == 0) atomicExch(err, 1);
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(Cfg::TMEM_COLS)
+                 : "memory");
+  }
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -284,9 +588,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D map over rows×cols (row stride ld elements) with 128-byte rows per box:
-// FP32 (box 32 × 128) or BF16 (box 64 × 128).
+// FP32 (box 32 × box_rows) or BF16 (box 64 × box_rows).
 static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld,
-                    bool bf16 = false) {
+                    bool bf16 = false, unsigned box_rows = 128) {
   auto fn = encode_fn();
   if (!fn) {
     set_last_error("gemm_tf32: cuTensorMapEncodeTiled unavailable");
@@ -294,7 +598,7 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t co
   }
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld * (bf16 ? 2 : 4))};
-  cuuint32_t box[2] = {(cuuint32_t)(bf16 ? 2 * kTcK : kTcK), 128u};
+  cuuint32_t box[2] = {(cuuint32_t)(bf16 ? 2 * kTcK : kTcK), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1u, 1u};
   CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                   2, const_cast<void*>(base), dims, strides,
@@ -314,6 +618,70 @@ __global__ void scale_c_kernel(int M, int N, float* C, int64_t ldc, float beta) 
   *p = (beta == 0.0f) ? 0.0f : beta * *p;
 }
 
+// 1 (default): C = alpha A Bᵀ + beta C runs on the persistent kernel when C
+// can be addressed by a tensor map; 0: one CTA per 128×128 tile.
+static int g_gemm_persistent = 1;
+
+// Persistent launch; returns -1 when C cannot be addressed by a tensor map
+// (the caller then uses the one-tile-per-CTA kernel).
+template <int MODE, class Cfg>
+static int gemm_persistent_cfg(int M, int N, int K, const void* A, const void* Al, int64_t lda,
+                               const void* B, const void* Bl, int64_t ldb, float* C, int64_t ldc,
+                               float alpha, float beta, int* err, cudaStream_t st) {
+  constexpr bool BF = MODE == 2;
+  if (!g_gemm_persistent) return -1;
+  if ((((uintptr_t)C) & 15) != 0 || (ldc % 4) != 0) return -1;
+  CUtensorMap ma, mb, mal, mbl, mc;
+  if (make_map(&mc, C, M, N, ldc, false, 32) != 0) {
+    cudaGetLastError();
+    return -1;
+  }
+  int rc = make_map(&ma, A, M, K, lda, BF, kTcM);
+  if (rc) return rc;
+  rc = make_map(&mb, B, N, K, ldb, BF, Cfg::BN);
+  if (rc) return rc;
+  mal = ma;
+  mbl = mb;
+  if (Cfg::SPLIT) {
+    rc = make_map(&mal, Al, M, K, lda, false, kTcM);
+    if (rc) return rc;
+    rc = make_map(&mbl, Bl, N, K, ldb, false, Cfg::BN);
+    if (rc) return rc;
+  }
+  const int64_t tiles = (int64_t)((M + kTcM - 1) / kTcM) * ((N + Cfg::BN - 1) / Cfg::BN);
+  const int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+  auto kern = gemm_nt_persistent_kernel<MODE, Cfg>;
+  LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::SMEM),
+                "gemm persistent: set smem");
+  kern<<<grid, kPThreads, Cfg::SMEM, st>>>(ma, mb, mal, mbl, mc, M, N, K, alpha, beta, err);
+  return check_launch("gemm persistent");
+}
+
+// K of at most two stages (beta != 0): the short-K configuration.
+template <int MODE>
+static int gemm_persistent(int M, int N, int K, const void* A, const void* Al, int64_t lda,
+                           const void* B, const void* Bl, int64_t ldb, float* C, int64_t ldc,
+                           float alpha, float beta, int* err, cudaStream_t st) {
+  const int kstage = MODE == 2 ? 2 * kTcK : kTcK;
+  const bool short_k = beta != 0.0f && K <= 2 * kstage;
+  if constexpr (MODE == 0) {
+    if (short_k)
+      return gemm_persistent_cfg<0, PCfgTf32ShortK>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc,
+                                                    alpha, beta, err, st);
+    return gemm_persistent_cfg<0, PCfgTf32>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc, alpha, beta,
+                                            err, st);
+  } else if constexpr (MODE == 2) {
+    if (short_k)
+      return gemm_persistent_cfg<2, PCfgBf16ShortK>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc,
+                                                    alpha, beta, err, st);
+    return gemm_persistent_cfg<2, PCfgBf16>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc, alpha, beta,
+                                            err, st);
+  } else {
+    return gemm_persistent_cfg<1, PCfgSplit>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc, alpha, beta,
+                                             err, st);
+  }
+}
+
 int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int64_t lda,
                        const float* B, const float* Bl, int64_t ldb, float* C, int64_t ldc,
                        float alpha, float beta, int* err, cudaStream_t st) {
@@ -324,6 +692,13 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
     return check_launch("gemm_tf32 (k = 0)");
   }
   const bool split = (Al != nullptr) && (Bl != nullptr);
+  {
+    const int prc = split ? gemm_persistent<1>(M, N, K, A, Al, lda, B, Bl, ldb, C, ldc, alpha,
+                                               beta, err, st)
+                          : gemm_persistent<0>(M, N, K, A, nullptr, lda, B, nullptr, ldb, C, ldc,
+                                               alpha, beta, err, st);
+    if (prc >= 0) return prc;
+  }
   CUtensorMap ma, mb, mal, mbl;
   int rc = make_map(&ma, A, M, K, lda);
   if (rc) return rc;
@@ -400,6 +775,11 @@ int gemm_bf16_nt(int M, int N, int K, const void* A, int64_t lda, const void* B,
     const int64_t total = (int64_t)M * N;
     scale_c_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(M, N, C, ldc, beta);
     return check_launch("gemm_bf16 (k = 0)");
+  }
+  {
+    const int prc = gemm_persistent<2>(M, N, K, A, nullptr, lda, B, nullptr, ldb, C, ldc, alpha,
+                                       beta, err, st);
+    if (prc >= 0) return prc;
   }
   CUtensorMap ma, mb;
   int rc = make_map(&ma, A, M, K, lda, true);
@@ -518,4 +898,9 @@ extern "C" int lxgb_gemm_bf16_nt(int32_t m, int32_t n, int32_t k, const void* a,
                  "gemm_bf16: A and B must be 16-byte aligned");
   }
   return gemm_bf16_nt(m, n, k, a, lda, b, ldb, c, ldc, alpha, beta, err, as_stream(stream));
+}
+
+extern "C" int lxgb_gemm_set_persistent(int32_t on) {
+  g_gemm_persistent = on ? 1 : 0;
+  return LXGB_SUCCESSFUL;
 }

@@ -114,3 +114,50 @@ def test_bf16_gemm_matches_reference(dev, m, n, k):
     r = c0.double() - a.double() @ b.double().T
     scale = (a.double().abs() @ b.double().abs().T) + c0.double().abs()
     assert float(((c.double() - r).abs() / scale).max()) <= (k + 2) * 2.0 ** -23
+
+
+def _run_mode(mode, a, b, c, alpha, beta):
+    from lineax_gb300 import _ffi
+
+    if mode == "tf32":
+        return _blas.gemm_tf32_nt(a, b, c, alpha=alpha, beta=beta)
+    if mode == "3xtf32":
+        return _blas.gemm_3xtf32_nt(a, b, c, alpha=alpha, beta=beta)
+    m, k = a.shape
+    n = b.shape[0]
+    ah, bh = a.to(torch.bfloat16).contiguous(), b.to(torch.bfloat16).contiguous()
+    err = torch.zeros(1, dtype=torch.int32, device=a.device)
+    _ffi.call("lxgb_gemm_bf16_nt", m, n, k, _ffi.ptr(ah), k, _ffi.ptr(bh), k, _ffi.ptr(c),
+              c.stride(0), float(alpha), float(beta), _ffi.ptr(err), _ffi.stream_handle(a.device))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    return c
+
+
+@pytest.mark.parametrize("mode", ["tf32", "3xtf32", "bf16"])
+@pytest.mark.parametrize("m,n,k,beta", [(4096, 4096, 64, 1.0), (2000, 3000, 96, 1.0),
+                                        (1100, 700, 304, 0.0), (4500, 520, 64, 0.5),
+                                        (129, 257, 40, 1.0)])
+def test_persistent_kernel_matches_tile_kernel(dev, mode, m, n, k, beta):
+    """The persistent GEMM (one CTA per SM, two tensor-memory accumulators,
+    several tiles per CTA at these sizes, ragged right and bottom tiles) gives
+    the values of the one-tile-per-CTA kernel: the same products accumulated
+    in the same K order, the same epilogue."""
+    from lineax_gb300 import _ffi
+
+    g = torch.Generator(device=dev).manual_seed(m + 3 * n + 7 * k)
+    a = torch.randn(m, k, device=dev, generator=g)
+    b = torch.randn(n, k, device=dev, generator=g)
+    c0 = torch.randn(m, n, device=dev, generator=g)
+    try:
+        _ffi.call("lxgb_gemm_set_persistent", 0)
+        tile = _run_mode(mode, a, b, c0.clone(), -1.0, beta)
+    finally:
+        _ffi.call("lxgb_gemm_set_persistent", 1)
+    pers = _run_mode(mode, a, b, c0.clone(), -1.0, beta)
+    torch.cuda.synchronize()
+    diff = float((pers.double() - tile.double()).abs().max())
+    scale = float(((a.double().abs() @ b.double().abs().T) + c0.double().abs()).max())
+    assert diff <= (k + 2) * 2.0 ** -23 * scale, (diff, scale)
+    print(f"{mode} {m}x{n}x{k} beta={beta}: max |persistent - tile| = {diff:.3e}"
+          f" ({'bit-identical' if diff == 0 else 'differs'})")
