@@ -66,6 +66,17 @@ int lxgb_getrf_batched_f64(int64_t batch, int32_t n, double* a, int64_t stride_a
                            int32_t* piv, int64_t stride_piv, int32_t* info,
                            void* stream);
 
+/* Kernel choice of lxgb_getrf_batched_f64 for 32 <= n <= 168 (a tuning
+ * switch, process-wide; factors, pivots and info are bit-identical either
+ * way): 1 factors each matrix on a cluster of two CTAs (columns split by
+ * parity, multipliers exchanged through distributed shared memory, one
+ * cluster barrier per column) when 2 * batch <= the SM count, so that small
+ * batches occupy twice as many SMs; 0 (the default) uses one CTA per matrix,
+ * whose pivot search for column k+1 overlaps the update of step k — faster on
+ * GB300, where the per-column cluster barrier costs more than the halved FP64
+ * work saves (0.33 ms against 0.44 ms for 64 matrices of order 128). */
+int lxgb_getrf_set_pair(int32_t on);
+
 /* Solve A_b X = B_b (trans = 0) or A_bᵀ X = B_b (trans = 1) in place on B
  * with the factor from lxgb_getrf_batched_f64.  B_b holds nrhs vectors of
  * length n at b + b*stride_b (vector r at offset r*n).

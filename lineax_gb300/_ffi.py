@@ -73,6 +73,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "lxgb_posv_mixed_small_max": (c_i32, []),
     "lxgb_posv_mixed_set_tensor_cores": (ctypes.c_int, [c_i32]),
     "lxgb_gemm_set_persistent": (ctypes.c_int, [c_i32]),
+    "lxgb_getrf_set_pair": (ctypes.c_int, [c_i32]),
     "lxgb_geqrf_t_elems": (c_i64, [c_i64]),
     "lxgb_geqrf_workspace_size": (c_i64, [c_i64, c_i64]),
     "lxgb_geqrf_f64": (ctypes.c_int, [c_i64, c_i64, c_p, c_i32, c_p, c_p, c_p, c_p, c_i64, c_p]),

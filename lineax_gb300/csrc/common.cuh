@@ -87,4 +87,26 @@ __device__ __forceinline__ void warp_argmax_first(double& v, int& idx) {
   }
 }
 
+// Pivot-search key of x: |x| as its IEEE bit pattern, which orders like the
+// value for every non-NaN x; NaN maps to -1 and never wins (as "|x| > v" never
+// holds for NaN).  64-bit integer compares run on the integer pipe, not on
+// GB300's narrow FP64 pipe.
+__device__ __forceinline__ long long pivot_key(double x) {
+  const long long b = __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL;
+  return b > 0x7FF0000000000000LL ? -1LL : b;
+}
+
+// warp_argmax_first over pivot keys.
+__device__ __forceinline__ void warp_argmax_first_key(long long& v, int& idx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && oi < idx)) {
+      v = ov;
+      idx = oi;
+    }
+  }
+}
+
 }  // namespace lxgb

@@ -36,6 +36,56 @@ def test_getrf_bit_exact_vs_getf2_twin(dev, n):
     assert np.array_equal(lu.cpu().numpy(), lu_ref), np.max(np.abs(lu.cpu().numpy() - lu_ref))
 
 
+@pytest.mark.parametrize("n,batch", [(128, 64), (33, 5), (167, 7), (168, 76)])
+def test_getrf_pair_cluster_bit_exact(dev, n, batch):
+    """With the switch on, batches of at most half the SM count run on two-CTA
+    clusters (columns split by parity between the CTAs): factors, pivots and
+    info equal the getf2 twin bit for bit, and equal the one-CTA kernel's."""
+    from lineax_gb300 import _ffi
+
+    rng = np.random.default_rng(n * 1000 + batch)
+    a = rng.standard_normal((batch, n, n)) / np.sqrt(n) + np.eye(n)
+    lu1, piv1, info1 = _dense.lu_factor_batched(t(a, dev))
+    try:
+        _ffi.call("lxgb_getrf_set_pair", 1)
+        lu, piv, info = _dense.lu_factor_batched(t(a, dev))
+    finally:
+        _ffi.call("lxgb_getrf_set_pair", 0)
+    lu_ref, piv_ref, info_ref = getf2_batched(a)
+    np.testing.assert_array_equal(piv.cpu().numpy(), piv_ref)
+    np.testing.assert_array_equal(info.cpu().numpy(), info_ref)
+    assert np.array_equal(lu.cpu().numpy(), lu_ref)
+    assert torch.equal(lu1, lu) and torch.equal(piv1, piv) and torch.equal(info1, info)
+
+
+def test_getrf_pair_cluster_singular_and_nan(dev):
+    """Zero pivots found by either CTA of the pair (info = the first one) and a
+    column of NaNs, against the getf2 twin, on both kernels."""
+    from lineax_gb300 import _ffi
+
+    rng = np.random.default_rng(5)
+    n = 64
+    a = rng.standard_normal((4, n, n)) + np.eye(n)
+    a[0, :, 10] = 0.0                   # zero column owned by CTA 0 (even)
+    a[1, :, 37] = 0.0                   # zero column owned by CTA 1 (odd)
+    a[2, :, 5] = 0.0
+    a[2, :, 20] = 0.0                   # two zero columns: info is the first
+    a[3, :, 12] = np.nan
+    lu_ref, piv_ref, info_ref = getf2_batched(a)
+    assert list(info_ref[:3]) == [11, 38, 6]
+    for pair in (1, 0):
+        try:
+            _ffi.call("lxgb_getrf_set_pair", pair)
+            lu, piv, info = _dense.lu_factor_batched(t(a, dev))
+        finally:
+            _ffi.call("lxgb_getrf_set_pair", 0)
+        np.testing.assert_array_equal(info.cpu().numpy(), info_ref)
+        np.testing.assert_array_equal(piv.cpu().numpy(), piv_ref)
+        got = lu.cpu().numpy()
+        assert np.array_equal(np.isnan(got), np.isnan(lu_ref))
+        assert np.array_equal(np.nan_to_num(got), np.nan_to_num(lu_ref))
+
+
 def test_getrf_pivots_match_lapack_config1(dev):
     """64 systems, n = 128, A = G/sqrt(n) + I: pivots equal LAPACK dgetrf's."""
     rng = np.random.default_rng(2024)
@@ -54,7 +104,7 @@ def test_getrf_zero_pivot_info(dev):
 
 
 @pytest.mark.parametrize("n,nrhs,trans", [(5, 1, 0), (64, 3, 1), (128, 1, 0), (300, 2, 1),
-                                          (777, 4, 0)])
+                                          (777, 4, 0), (33, 9, 0), (160, 11, 1), (168, 2, 0)])
 def test_lu_solve_backward_error(dev, n, nrhs, trans):
     rng = np.random.default_rng(7 + n)
     a = rng.standard_normal((n, n)) / np.sqrt(n) + np.eye(n)
