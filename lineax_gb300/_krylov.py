@@ -6,7 +6,8 @@ lineax/_solver/gmres.py:106-413; every vector operation and reduction of the
 loop body runs in liblxgb.so (lxgb_cg_* / lxgb_gmres_*).  Operator and
 preconditioner products are formed here: MatrixLinearOperator through
 lxgb_gemv_f64, operators with a ``mv_block`` method (e.g. the Poisson stencil)
-on a whole (k, n) block, and other FunctionLinearOperators vector by vector.
+on a whole (k, n) block, and other FunctionLinearOperators through torch.vmap
+(vector by vector when the function cannot be batched).
 Each right-hand side has device-side flags, so the host checks convergence
 only every few iterations; iterations past a right-hand side's stop leave it
 untouched, which makes every right-hand side's result the same as when it is
@@ -28,7 +29,7 @@ import torch
 
 from . import _blas, _ffi
 from ._operator import IdentityLinearOperator, MatrixLinearOperator
-from ._structure import ravel, tree_flatten, unravel
+from ._structure import ravel, tree_flatten
 
 SUCCESSFUL, MAX_STEPS_REACHED, SINGULAR, BREAKDOWN, STAGNATION = 0, 1, 2, 3, 4
 EPS64 = 2.220446049250313e-16
@@ -52,9 +53,9 @@ def block_mv(operator, x: torch.Tensor) -> torch.Tensor:
         return _blas.gemv(operator.matrix, x)
     if hasattr(operator, "mv_block"):
         return operator.mv_block(x)
-    ins = operator.in_structure()
-    rows = [ravel(operator.mv(unravel(x[c], ins)), torch.float64) for c in range(x.shape[0])]
-    return torch.stack(rows).contiguous()
+    from ._operator import apply_columns
+
+    return apply_columns(operator, x).to(torch.float64).contiguous()
 
 
 def device_operator(operator):

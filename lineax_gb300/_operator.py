@@ -85,14 +85,21 @@ class MatrixLinearOperator(AbstractLinearOperator):
     def __init__(self, matrix: torch.Tensor, tags=()):
         if not isinstance(matrix, torch.Tensor) or matrix.ndim != 2:
             raise ValueError("`MatrixLinearOperator(matrix=...)` should be 2-dimensional.")
-        if matrix.is_complex():
-            raise ValueError("complex dtypes are not supported by lineax_gb300")
-        if not torch.is_floating_point(matrix):
+        if not torch.is_floating_point(matrix) and not matrix.is_complex():
             matrix = matrix.to(torch.get_default_dtype())
         self.matrix = matrix
         self.tags = _frozenset(tags)
+        self._real = None   # real form of a complex matrix, built on first use
 
     def mv(self, vector):
+        if self.matrix.is_complex() or (isinstance(vector, torch.Tensor) and vector.is_complex()):
+            # complex product through the real form R(A) [Re x; Im x]
+            from . import _complex
+
+            if self._real is None:
+                self._real = _complex.real_form_matrix(self.matrix)
+            y = _blas.gemv(self._real, _complex.to_real(vector))
+            return _complex.from_real(y)
         return _blas.gemv(self.matrix, vector)
 
     def as_matrix(self):
@@ -128,7 +135,7 @@ class FunctionLinearOperator(AbstractLinearOperator):
         return materialise(self).matrix
 
     def transpose(self):
-        if symmetric_tag in self.tags:
+        if is_symmetric(self):
             return self
         return materialise(self).transpose()
 
@@ -268,9 +275,17 @@ class TaggedLinearOperator(AbstractLinearOperator):
 
 
 def is_symmetric(op) -> bool:
+    """Aᵀ = A: tagged symmetric or diagonal, or (real dtypes only) positive or
+    negative semidefinite — for complex operators those tags mean Hermitian
+    (lineax/_operator.py:1617-1631)."""
     t = op.tags
-    return any(x in t for x in (symmetric_tag, positive_semidefinite_tag,
-                                negative_semidefinite_tag, diagonal_tag))  # real dtypes only
+    if symmetric_tag in t or diagonal_tag in t:
+        return True
+    if positive_semidefinite_tag in t or negative_semidefinite_tag in t:
+        from ._complex import operator_is_complex
+
+        return not operator_is_complex(op)
+    return False
 
 
 def is_diagonal(op) -> bool:
@@ -306,9 +321,42 @@ def linearise(op):
     return op
 
 
+def apply_columns(op, x: torch.Tensor) -> torch.Tensor:
+    """op applied to every row of the (k, n) block x, as one batched call: a
+    GEMM for matrices, the operator's own block product when it has one (the
+    Poisson stencil, compositions, tagged and negated operators), and
+    torch.vmap of the function for FunctionLinearOperator (the counterpart of
+    the jax.vmap in lineax/_operator.py:1369-1388).  A function that torch.vmap
+    cannot batch (one that calls out of torch) is applied row by row."""
+    if isinstance(op, MatrixLinearOperator):
+        if op.matrix.is_complex() or x.is_complex():
+            return op.mv(x)
+        return _blas.gemv(op.matrix, x)
+    if isinstance(op, IdentityLinearOperator):
+        return x
+    if isinstance(op, NegLinearOperator):
+        return -apply_columns(op.operator, x)
+    if isinstance(op, ComposedLinearOperator):
+        return apply_columns(op.outer, apply_columns(op.inner, x))
+    if isinstance(op, TaggedLinearOperator):
+        return apply_columns(op.operator, x)
+    if hasattr(op, "mv_block"):
+        return op.mv_block(x)
+    ins, outs = op.in_structure(), op.out_structure()
+    out_dtype = tree_flatten(outs)[0][0].dtype
+
+    def one(row):
+        return ravel(op.mv(unravel(row, ins)), out_dtype)
+
+    try:
+        return torch.vmap(one)(x).contiguous()
+    except Exception:  # noqa: BLE001 - functions outside torch's batching rules
+        return torch.stack([one(x[c]) for c in range(x.shape[0])]).contiguous()
+
+
 def materialise(op) -> MatrixLinearOperator:
     """Turn an operator into a MatrixLinearOperator by applying it to the
-    columns of the identity (lineax/_operator.py:1369-1388)."""
+    columns of the identity in one batched call (lineax/_operator.py:1369-1388)."""
     if isinstance(op, MatrixLinearOperator):
         return op
     ins = op.in_structure()
@@ -316,13 +364,13 @@ def materialise(op) -> MatrixLinearOperator:
     dtype = leaves[0].dtype
     n = tree_size(ins)
     eye = torch.eye(n, dtype=dtype, device="cuda")
-    cols = [ravel(op.mv(unravel(eye[j], ins)), dtype) for j in range(n)]
-    return MatrixLinearOperator(torch.stack(cols, dim=1).contiguous(), op.tags)
+    rows = apply_columns(op, eye)            # row j = op(e_j)
+    return MatrixLinearOperator(rows.T.contiguous(), op.tags)
 
 
 def conj_not_needed(state, options):
     """conj of a solver state over real operators is the state itself (complex
-    dtypes are rejected when the operator is built)."""
+    operators are solved through real forms, whose states are real)."""
     return state, options
 
 

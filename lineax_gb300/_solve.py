@@ -12,6 +12,7 @@ a Solution.
 from __future__ import annotations
 
 import abc
+import contextlib
 from typing import Any
 
 import torch
@@ -171,6 +172,8 @@ class AutoLinearSolver(AbstractLinearSolver):
 
 def _any_nonfinite(tree) -> bool:
     leaves, _ = tree_flatten(tree)
+    leaves = [torch.view_as_real(x.to(torch.complex128)) if x.is_complex() else x
+              for x in leaves]
     flags = [_blas.any_nonfinite(x) for x in leaves if x.numel() > 0]
     if not flags:
         return False
@@ -216,9 +219,7 @@ def linear_solve(
     for x in leaves:
         if not isinstance(x, torch.Tensor):
             x = torch.as_tensor(x, device="cuda")
-        if x.is_complex():
-            raise ValueError("complex dtypes are not supported by lineax_gb300")
-        if not torch.is_floating_point(x):
+        if not torch.is_floating_point(x) and not x.is_complex():
             x = x.to(torch.get_default_dtype())
         fixed.append(x)
     from ._structure import tree_unflatten
@@ -232,12 +233,30 @@ def linear_solve(
         )
     if isinstance(operator, IdentityLinearOperator):
         return Solution(value=vector, result=RESULTS.successful, state=state, stats={})
-    if state is sentinel:
-        state = solver.init(operator, options)
-    solution, result, stats = solver.compute(state, vector, options)
+    from . import _complex
+
+    if _complex.operator_is_complex(operator) or _complex.tree_is_complex(vector):
+        # complex problems run on real forms of the operator (see _complex)
+        solution, result, stats, state = _complex.linear_solve_complex(
+            operator, vector, solver, options, state, sentinel)
+        result = _finalize(solution, int(result), vector)
+        if throw and result != RESULTS.successful:
+            raise LinearSolveError(result)
+        return Solution(value=solution, result=result, state=state, stats=stats)
+    from . import _autodiff
+
+    diff = _autodiff.needs_grad(operator, vector)
+    with torch.no_grad() if diff else contextlib.nullcontext():
+        if state is sentinel:
+            state = solver.init(operator, options)
+        solution, result, stats = solver.compute(state, vector, options)
     result = _finalize(solution, int(result), vector)
     if throw and result != RESULTS.successful:
         raise LinearSolveError(result)
+    if diff:
+        # derivative rules of lineax/_solve.py:151-317 (see _autodiff)
+        solution = _autodiff.differentiable(
+            operator, vector, solution, _autodiff.SolveContext(operator, solver, state, options))
     return Solution(value=solution, result=result, state=state, stats=stats)
 
 

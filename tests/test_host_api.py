@@ -95,19 +95,50 @@ def test_identity_operator_short_circuit():
     assert sol.value is v and sol.result == lx.RESULTS.successful
 
 
-def test_complex_inputs_are_rejected():
-    """Complex dtypes are out of scope: building an operator from a complex
-    matrix, or solving for a complex vector, raises instead of dropping the
-    imaginary part."""
+def test_complex_real_forms():
+    """Complex problems are solved through real forms (lineax_gb300._complex):
+    R(A) [Re x; Im x] = [Re Ax; Im Ax], Hermitian definiteness maps to
+    symmetric definiteness, and the diagonal-scaled interleaved form of a
+    triangular matrix is unit triangular with the same solution."""
     import pytest
     import torch
 
     import lineax_gb300 as lx
+    from lineax_gb300 import _complex
 
-    with pytest.raises(ValueError, match="complex"):
-        lx.MatrixLinearOperator(torch.eye(3, dtype=torch.complex128))
+    g = torch.Generator().manual_seed(3)
+    a = torch.randn(5, 4, dtype=torch.complex128, generator=g)
+    x = torch.randn(4, dtype=torch.complex128, generator=g)
+    r = _complex.real_form_matrix(a)
+    assert r.dtype == torch.float64 and r.shape == (10, 8)
+    assert torch.allclose(r @ _complex.to_real(x), _complex.to_real(a @ x))
+    assert torch.allclose(_complex.from_real(_complex.to_real(x)), x)
+    # Hermitian positive definite A: R(A) symmetric positive definite
+    h = a.conj().T @ a + torch.eye(4, dtype=torch.complex128)
+    rh = _complex.real_form_matrix(h)
+    assert torch.allclose(rh, rh.T) and bool((torch.linalg.eigvalsh(rh) > 0).all())
+    tags = _complex.real_form_tags({lx.positive_semidefinite_tag})
+    assert tags == {lx.positive_semidefinite_tag, lx.symmetric_tag}
+    assert _complex.real_form_tags({lx.symmetric_tag, lx.lower_triangular_tag}) == frozenset()
+    # complex PSD means Hermitian, not symmetric (lineax/_operator.py:1617-1631)
+    assert not lx.is_symmetric(lx.MatrixLinearOperator(h, lx.positive_semidefinite_tag))
+    assert lx.is_symmetric(lx.MatrixLinearOperator(h.real, lx.positive_semidefinite_tag))
+    # triangular: D^-1 T in interleaved real form is unit lower triangular
+    t = torch.tril(torch.randn(4, 4, dtype=torch.complex128, generator=g)) + 3 * torch.eye(4)
+    d = torch.diagonal(t)
+    ts = t / d[:, None]
+    e = torch.zeros(8, 8, dtype=torch.float64)
+    e[0::2, 0::2], e[0::2, 1::2] = ts.real, -ts.imag
+    e[1::2, 0::2], e[1::2, 1::2] = ts.imag, ts.real
+    assert torch.allclose(torch.triu(e, 1), torch.zeros_like(e), atol=1e-15)
+    assert torch.allclose(torch.diagonal(e), torch.ones(8, dtype=torch.float64))
+    xt = torch.randn(4, dtype=torch.complex128, generator=g)
+    inter = torch.stack([xt.real, xt.imag], 1).reshape(-1)
+    rhs = (t @ xt) / d
+    assert torch.allclose(e @ inter, torch.stack([rhs.real, rhs.imag], 1).reshape(-1))
+    # a complex vector for a real operator is a structure mismatch, as in lineax
     op = lx.MatrixLinearOperator(torch.eye(3, dtype=torch.float64))
-    with pytest.raises(ValueError, match="complex"):
+    with pytest.raises(ValueError, match="structures do not match"):
         lx.linear_solve(op, torch.ones(3, dtype=torch.complex128), lx.LU())
 
 
