@@ -406,11 +406,11 @@ def run_gpu(args):
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak,
             # DRAM bytes per launch from one ncu capture of this 4096-system
-            # launch: 3985.4 MB read + 1039.7 MB written (A is read by the
+            # launch: 3964.1 MB read + 930.3 MB written (A is read by the
             # FP32 copy and by each refinement residual; factor slices of
             # large systems spill from L2); scaled by the algorithmic bytes
             # when --systems changes the workload.
-            "traffic": 5025.0e6 * hbm_bytes / 1215167544.0,
+            "traffic": 4894.4e6 * hbm_bytes / 1215167544.0,
             "kernel": "posv_mixed_kernel",
             "note": "HBM roofline of the algorithmic bytes (A read once, b, x); the kernel is "
                     "latency-bound (barriers, shared-memory and FP latency at 16 warps per "
