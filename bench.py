@@ -886,8 +886,8 @@ def run_cg_poisson(args):
     print(json.dumps(out), flush=True)
 
 
-SERVE_ROUTES = ("chol_ragged", "lu_small", "lu_mixed", "qr_mixed", "qr_f64", "lu_f64",
-                "chol_f64")
+SERVE_ROUTES = ("chol_ragged", "lu_small", "lu_mixed", "chol_mixed", "qr_mixed", "qr_f64",
+                "lu_f64", "chol_f64")
 
 
 def serve_suite(args, dev, loads=(0.25, 0.5, 0.75), emit=None):

@@ -541,6 +541,34 @@ int lxgb_getrf_f32_tc(int32_t n, const double* a64, float* lu, int32_t* piv,
                       int32_t* info, int32_t precision, int32_t* err,
                       void* work, int64_t work_bytes, void* stream);
 
+/* FP32 Cholesky A = L Lᵀ of one SPD matrix (row-major n×n FP64, read from
+ * its upper triangle as lineax's cho_factor(lower=False) reads it; n % 4 == 0,
+ * n < 32768) for mixed-precision refinement: l (n×n FP32, 16-byte aligned)
+ * receives L in its lower triangle (the upper triangle is scratch).  64-column
+ * panels: the diagonal block factored by one CTA, the panel below it by FP32
+ * substitution (one row per thread), the trailing update on the tiles of the
+ * lower triangle as a tcgen05 GEMM with 3xTF32 products.  *info = 0, or the 1-based index of the first pivot that is not
+ * positive in FP32 (the factor is then unusable); *err is set if a tensor-core
+ * pipeline wait gave up.  work 256-byte aligned, work_bytes >=
+ * lxgb_potrf_f32_tc_workspace_size(n).  The low-precision counterpart of
+ * cho_factor at lineax/_solver/cholesky.py:60. */
+int64_t lxgb_potrf_f32_tc_workspace_size(int64_t n);
+int lxgb_potrf_f32_tc(int64_t n, const double* a, float* l, int32_t* info,
+                      int32_t* err, void* work, int64_t work_bytes, void* stream);
+
+/* The factor of lxgb_potrf_f32_tc in the form of lxgb_getrf_f32_tc (L' =
+ * L D^{-1} unit lower below the diagonal, U' = D Lᵀ on and above it, D =
+ * diag(L)) with piv = 0..n-1, so that lxgb_lu32_inverse and GMRES-IR apply
+ * to it unchanged.  l and lu may not alias. */
+int lxgb_chol32_to_lu32(int64_t n, const float* l, float* lu, int32_t* piv,
+                        void* stream);
+
+/* uinv = U'^{-1} = L'^{-T} D^{-2} from linv = L'^{-1} (lxgb_lu32_inverse with
+ * uinv NULL) and lu from lxgb_chol32_to_lu32 (D^2 on its diagonal): the second
+ * triangular inverse of a Cholesky factor by a transposing copy. */
+int lxgb_chol32_uinv(int64_t n, const float* lu, const float* linv, float* uinv,
+                     void* stream);
+
 /* x_r = U^{-1} L^{-1} P b_r for nrhs FP64 vectors (length n, back to back),
  * computed in FP32 with a factor from lxgb_getrf_f32_tc: the preconditioner
  * apply of GMRES-IR.  b and x may not alias. */
@@ -548,8 +576,9 @@ int lxgb_getrs_f32(int32_t n, int32_t nrhs, const float* lu, const int32_t* piv,
                    const double* b, double* x, void* stream);
 
 /* Inverse factors of a factor from lxgb_getrf_f32_tc: linv = L^{-1} (unit
- * lower, zeros above the diagonal) and uinv = U^{-1} (zeros below), both
- * row-major n×n FP32, and perm with (P b)_i = b[perm[i]].  Off-diagonal
+ * lower, zeros above the diagonal) and uinv = U^{-1} (zeros below; uinv may
+ * be NULL, then only L^{-1} is formed), both row-major n×n FP32, and perm with
+ * (P b)_i = b[perm[i]].  Off-diagonal
  * updates on the tensor cores: precision 0 TF32, 1 3xTF32.  n <= 25600,
  * n % 4 == 0, lu 16-byte and work 256-byte aligned, work_bytes >=
  * lxgb_lu32_inverse_workspace_size.  *err is set if a tensor-core pipeline

@@ -139,6 +139,10 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
                                          c_i64, c_p]),
     "lxgb_cg32_status": (ctypes.c_int, [c_i32, c_p, c_p, c_i64, c_p]),
     "lxgb_lu32_inverse_workspace_size": (c_i64, [c_i32, c_i32]),
+    "lxgb_potrf_f32_tc_workspace_size": (c_i64, [c_i64]),
+    "lxgb_potrf_f32_tc": (ctypes.c_int, [c_i64, c_p, c_p, c_p, c_p, c_p, c_i64, c_p]),
+    "lxgb_chol32_to_lu32": (ctypes.c_int, [c_i64, c_p, c_p, c_p, c_p]),
+    "lxgb_chol32_uinv": (ctypes.c_int, [c_i64, c_p, c_p, c_p, c_p]),
     "lxgb_lu32_inverse": (ctypes.c_int, [c_i32, c_p, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64,
                                          c_p]),
     "lxgb_lu32_apply_workspace_size": (c_i64, [c_i32, c_i32]),

@@ -320,6 +320,23 @@ static_assert(PCfgTf32::SMEM <= 232448 && PCfgTf32ShortK::SMEM <= 232448 &&
                   PCfgBf16ShortK::SMEM <= 232448,
               "persistent GEMM exceeds shared memory");
 
+// Lower mode (C symmetric, only its lower triangle wanted): the tiles that
+// hold a part of the lower triangle, row block by row block.
+__device__ __forceinline__ int lower_tiles_in_row(int mb, int n_nblk, int bn) {
+  return min(n_nblk, (mb * 128 + 127) / bn + 1);
+}
+
+__device__ __forceinline__ void tile_coords_lower(int tile, int n_mblk, int n_nblk, int bn,
+                                                  int& mb, int& nb) {
+  mb = 0;
+  for (; mb < n_mblk - 1; ++mb) {
+    const int c = lower_tiles_in_row(mb, n_nblk, bn);
+    if (tile < c) break;
+    tile -= c;
+  }
+  nb = tile;
+}
+
 __device__ __forceinline__ void tile_coords(int tile, int n_mblk, int n_nblk, int& mb, int& nb) {
   constexpr int G = 8;
   const int per_group = G * n_nblk;
@@ -338,7 +355,7 @@ gemm_nt_persistent_kernel(const __grid_constant__ CUtensorMap map_a,
                           const __grid_constant__ CUtensorMap map_al,
                           const __grid_constant__ CUtensorMap map_bl,
                           const __grid_constant__ CUtensorMap map_c, int M, int N, int K,
-                          float alpha, float beta, int* err) {
+                          float alpha, float beta, int* err, int lower) {
   constexpr bool SPLIT = Cfg::SPLIT;
   constexpr bool BF = MODE == 2;
   constexpr int BN = Cfg::BN, S = Cfg::S;
@@ -359,7 +376,17 @@ gemm_nt_persistent_kernel(const __grid_constant__ CUtensorMap map_a,
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_mblk = (M + kTcM - 1) / kTcM, n_nblk = (N + BN - 1) / BN;
-  const int tiles = n_mblk * n_nblk;
+  int tiles = n_mblk * n_nblk;
+  if (lower) {
+    tiles = 0;
+    for (int mb = 0; mb < n_mblk; ++mb) tiles += lower_tiles_in_row(mb, n_nblk, BN);
+  }
+  auto coords = [&](int tile, int& mb, int& nb) {
+    if (lower)
+      tile_coords_lower(tile, n_mblk, n_nblk, BN, mb, nb);
+    else
+      tile_coords(tile, n_mblk, n_nblk, mb, nb);
+  };
   const int ktiles = (K + kK - 1) / kK;
 
   if (threadIdx.x == 0) {
@@ -387,7 +414,7 @@ gemm_nt_persistent_kernel(const __grid_constant__ CUtensorMap map_a,
       int it = 0;
       for (int tile = blockIdx.x; tile < tiles && !*vabort; tile += gridDim.x) {
         int mb, nb;
-        tile_coords(tile, n_mblk, n_nblk, mb, nb);
+        coords(tile, mb, nb);
         for (int t = 0; t < ktiles; ++t, ++it) {
           const int s = it % S, r = it / S;
           if (!mbar_wait(&empty[s], (r & 1) ^ 1)) { atomicExch(abort_flag, 1); break; }
@@ -468,7 +495,7 @@ gemm_nt_persistent_kernel(const __grid_constant__ CUtensorMap map_a,
       if (c >= kChunks) { c -= kChunks; tile += gridDim.x; }
       if (tile >= tiles) return false;
       int mb, nb;
-      tile_coords(tile, n_mblk, n_nblk, mb, nb);
+      coords(tile, mb, nb);
       x = nb * BN + 32 * c;
       y = mb * kTcM + 32 * q;
       return x < N && y < M;   // chunks wholly outside C are skipped
@@ -627,7 +654,8 @@ static int g_gemm_persistent = 1;
 template <int MODE, class Cfg>
 static int gemm_persistent_cfg(int M, int N, int K, const void* A, const void* Al, int64_t lda,
                                const void* B, const void* Bl, int64_t ldb, float* C, int64_t ldc,
-                               float alpha, float beta, int* err, cudaStream_t st) {
+                               float alpha, float beta, int* err, cudaStream_t st,
+                               int lower = 0) {
   constexpr bool BF = MODE == 2;
   if (!g_gemm_persistent) return -1;
   if ((((uintptr_t)C) & 15) != 0 || (ldc % 4) != 0) return -1;
@@ -653,7 +681,8 @@ static int gemm_persistent_cfg(int M, int N, int K, const void* A, const void* A
   auto kern = gemm_nt_persistent_kernel<MODE, Cfg>;
   LXGB_CUDA_TRY(ensure_dynamic_smem(reinterpret_cast<const void*>(kern), Cfg::SMEM),
                 "gemm persistent: set smem");
-  kern<<<grid, kPThreads, Cfg::SMEM, st>>>(ma, mb, mal, mbl, mc, M, N, K, alpha, beta, err);
+  kern<<<grid, kPThreads, Cfg::SMEM, st>>>(ma, mb, mal, mbl, mc, M, N, K, alpha, beta, err,
+                                           lower);
   return check_launch("gemm persistent");
 }
 
@@ -734,6 +763,30 @@ int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int
                                                           N, K, C, ldc, alpha, beta, err, 0, 0);
   }
   return check_launch("gemm_tf32");
+}
+
+// C = alpha A Aᵀ + beta C on the tiles that hold C's lower triangle (C is
+// M×M and symmetric, A M×K; 3xTF32 when Al is given).  Tiles on the diagonal
+// are computed whole, so C's upper triangle is left partly updated.  Falls
+// back to the full product when the persistent kernel is off or C cannot be
+// addressed by a tensor map.
+int gemm_tf32_nt_split_lower(int M, int K, const float* A, const float* Al, int64_t lda, float* C,
+                             int64_t ldc, float alpha, float beta, int* err, cudaStream_t st) {
+  if (M <= 0) return LXGB_SUCCESSFUL;
+  if (K > 0) {
+    int prc;
+    if (Al != nullptr)
+      prc = gemm_persistent_cfg<1, PCfgSplit>(M, M, K, A, Al, lda, A, Al, lda, C, ldc, alpha,
+                                              beta, err, st, 1);
+    else if (beta != 0.0f && K <= 2 * kTcK)
+      prc = gemm_persistent_cfg<0, PCfgTf32ShortK>(M, M, K, A, nullptr, lda, A, nullptr, lda, C,
+                                                   ldc, alpha, beta, err, st, 1);
+    else
+      prc = gemm_persistent_cfg<0, PCfgTf32>(M, M, K, A, nullptr, lda, A, nullptr, lda, C, ldc,
+                                             alpha, beta, err, st, 1);
+    if (prc >= 0) return prc;
+  }
+  return gemm_tf32_nt_split(M, M, K, A, Al, lda, A, Al, lda, C, ldc, alpha, beta, err, st);
 }
 
 int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb,

@@ -11,6 +11,10 @@ int gemm_tf32_nt(int M, int N, int K, const float* A, int64_t lda, const float* 
 int gemm_tf32_nt_split(int M, int N, int K, const float* A, const float* Al, int64_t lda,
                        const float* B, const float* Bl, int64_t ldb, float* C, int64_t ldc,
                        float alpha, float beta, int* err, cudaStream_t st);
+// C = alpha A Aᵀ + beta C on the tiles holding C's lower triangle (M×M),
+// 3xTF32 when Al is given; the full product when tiles cannot be skipped.
+int gemm_tf32_nt_split_lower(int M, int K, const float* A, const float* Al, int64_t lda, float* C,
+                             int64_t ldc, float alpha, float beta, int* err, cudaStream_t st);
 // X = L_jj^{-1} W on rows [j0, j0+nb) of w, columns [c_begin, c_end), L_jj
 // the unit-lower 64-block of lu at (j0, j0) (row stride n; lu and w may be
 // the same array when the columns are disjoint from the block).  X goes back

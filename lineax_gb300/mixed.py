@@ -69,6 +69,57 @@ def lu_factor_tf32(a: torch.Tensor, precision: str = "tf32") -> LU32:
     return LU32(lu, piv, info)
 
 
+def cholesky_factor_tf32(a: torch.Tensor) -> LU32:
+    """FP32 Cholesky A = L Lᵀ with 3xTF32 tensor-core updates
+    (lxgb_potrf_f32_tc; A read from its upper triangle), returned in the
+    unit-lower / upper form of lu_factor_tf32 (L' = L D⁻¹, U' = D Lᵀ, no
+    interchanges) so that gmres_ir applies unchanged.  info > 0 when a pivot
+    is not positive in FP32."""
+    a64 = as_device_f64(a)
+    n = a64.shape[0]
+    if a64.shape != (n, n):
+        raise ValueError("cholesky_factor_tf32 needs a square matrix")
+    if n % 4:
+        raise ValueError("cholesky_factor_tf32 needs n to be a multiple of 4")
+    dev = a64.device
+    l = torch.empty((n, n), dtype=torch.float32, device=dev)
+    lu = torch.empty((n, n), dtype=torch.float32, device=dev)
+    piv = torch.empty(n, dtype=torch.int32, device=dev)
+    info = torch.empty(1, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    wbytes = int(_ffi.load().lxgb_potrf_f32_tc_workspace_size(n))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    s = _ffi.stream_handle(dev)
+    _ffi.call("lxgb_potrf_f32_tc", n, _ffi.ptr(a64), _ffi.ptr(l), _ffi.ptr(info), _ffi.ptr(err),
+              _ffi.ptr(work), work.numel() * 8, s)
+    _ffi.call("lxgb_chol32_to_lu32", n, _ffi.ptr(l), _ffi.ptr(lu), _ffi.ptr(piv), s)
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the Cholesky update")
+    return LU32(lu, piv, info)
+
+
+def cholesky_inverse(factor: LU32) -> InverseLU32:
+    """Triangular inverses of a factor from cholesky_factor_tf32: L'⁻¹ by the
+    tensor-core substitution of lu_inverse, U'⁻¹ = L'⁻ᵀ D⁻² by a transposing
+    copy (no second substitution)."""
+    lu = factor.lu
+    n = lu.shape[0]
+    dev = lu.device
+    linv = torch.empty((n, n), dtype=torch.float32, device=dev)
+    uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, 1))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    s = _ffi.stream_handle(dev)
+    _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(lu), _ffi.ptr(factor.piv), _ffi.ptr(linv), None,
+              _ffi.ptr(perm), 1, _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8, s)
+    _ffi.call("lxgb_chol32_uinv", n, _ffi.ptr(lu), _ffi.ptr(linv), _ffi.ptr(uinv), s)
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
+    return InverseLU32(linv, uinv, perm)
+
+
 class LUPreconditioner(AbstractLinearOperator):  # noqa: D101
     """M = (P^T L U)^{-1} applied in FP32 to FP64 vectors (lxgb_getrs_f32)."""
 

@@ -23,22 +23,29 @@ the HBM budget, and runs them grouped by route:
                distinct order (each system's arithmetic is the same as alone;
                right-hand-side blocks are zero padded, and each vector is
                solved independently).
-  lu_mixed     LU requests above that, and Cholesky requests with n > 1024:
-               FP32 LU with 3xTF32 tensor-core updates, its triangular
-               inverses, refinement to FP64 backward error (lineax_gb300.mixed:
-               plain refinement, then GMRES-IR, then FP64 LU when refinement
-               stalls); factor, inverses and the split A stay resident.
-  qr_mixed     QR requests with n > 168: FP32 Householder QR with TF32
+  lu_mixed     LU requests with n >= 512 (MIXED_MIN_N; between 169 and 511
+               the mixed server uses lu_f64, which is faster there): FP32 LU
+               with 3xTF32 tensor-core
+               updates, its triangular inverses, refinement to FP64 backward
+               error (lineax_gb300.mixed: plain refinement, then GMRES-IR, then
+               FP64 LU when refinement stalls); factor, inverses and the split
+               A stay resident.
+  chol_mixed   Cholesky requests with n > 1024: FP32 Cholesky with 3xTF32
+               tensor-core updates (no pivoting, lower-triangle trailing
+               updates), L'⁻¹ on the tensor cores and U'⁻¹ by a transposing
+               copy, then the same refinement; an operator that is not
+               positive definite in FP32 is factored by the mixed LU instead.
+  qr_mixed     QR requests with n >= 512: FP32 Householder QR with TF32
                tensor-core updates and Q formed explicitly, R^{-1} on the
                tensor cores, GMRES-IR preconditioned by R^{-1} Qᵀ (FP64 QR
                when refinement stalls); Qᵀ, R^{-1} and the split A stay
                resident.
-  qr_f64       QR requests with n <= 168 (both modes) and every QR request in
+  qr_f64       QR requests with n < 512 (both modes) and every QR request in
                FP64 mode: FP64 Householder QR (lineax's QR solver), the
                factor resident.
-  lu_f64 / chol_f64   FP64 mode above n = 168 (LU) and 1024 (Cholesky,
-               multi-CTA FP64 factor): the plain FP64 GPU path with resident
-               factors.
+  lu_f64 / chol_f64   LU above n = 168 (in mixed mode up to 511) and, in FP64
+               mode, Cholesky above 1024 (multi-CTA FP64 factor): the plain
+               FP64 GPU path with resident factors.
 
 Serving is continuous: run() keeps admitting requests as they arrive and as
 memory frees up while earlier work is still on the GPU.  Admitted work goes
@@ -73,6 +80,12 @@ from . import _blas, _dense, _ffi, batched, mixed
 KINDS = ("lu", "cholesky", "qr")
 SMALL_LU_MAX = 168      # one CTA per system, matrix in shared memory
 RAGGED_CHOL_MAX = 1024  # the ragged mixed-precision Cholesky kernel's limit
+# Below this order the FP64 LU and QR finish a request sooner than the mixed
+# path's factor, inverses and refinement (measured on GB300 by order bucket:
+# 169-255 LU 1.05 vs 1.85 ms, QR 2.7 vs 4.5 ms; 256-511 LU 2.05 vs 2.5 ms, QR
+# 4.4 vs 4.6 ms; from 512 the mixed path wins), so the mixed server sends
+# those requests to the FP64 routes.
+MIXED_MIN_N = 512
 
 
 @dataclasses.dataclass
@@ -111,12 +124,12 @@ def route_of(kind: str, n: int, mode: str) -> str:
     if kind == "cholesky":
         if n <= RAGGED_CHOL_MAX:
             return "chol_ragged"
-        return "lu_mixed" if mode == "mixed" else "chol_f64"
+        return "chol_mixed" if mode == "mixed" else "chol_f64"
     if kind == "qr":
-        return "qr_mixed" if (mode == "mixed" and n > SMALL_LU_MAX) else "qr_f64"
+        return "qr_mixed" if (mode == "mixed" and n >= MIXED_MIN_N) else "qr_f64"
     if n <= SMALL_LU_MAX:
         return "lu_small"
-    return "lu_mixed" if mode == "mixed" else "lu_f64"
+    return "lu_mixed" if (mode == "mixed" and n >= MIXED_MIN_N) else "lu_f64"
 
 
 def footprint(route: str, n: int, nrhs: int) -> int:
@@ -137,7 +150,7 @@ def footprint(route: str, n: int, nrhs: int) -> int:
 def resident_bytes(route: str, n: int) -> int:
     """Bytes of what stays resident for an operator between requests."""
     n4 = (n + 3) // 4 * 4
-    if route == "lu_mixed":
+    if route in ("lu_mixed", "chol_mixed"):
         # A (FP64), FP32 factor, both triangular inverses, A as a hi + lo pair
         return 8 * n4 * n4 + 4 * n4 * n4 + 8 * n4 * n4 + 8 * n4 * n4
     if route == "qr_mixed":
@@ -464,6 +477,27 @@ class SolveServer:
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "lu_mixed", ir.fallback, reused)
 
+    def _run_chol_mixed(self, req: Request) -> Completion:
+        res = self._acquire(req.op_id)
+        reused = res is not None
+        n4 = (req.n + 3) // 4 * 4
+        if res is None:
+            ap = _pad_identity(self._matrix(req), n4)
+            f = mixed.cholesky_factor_tf32(ap)
+            if int(f.info.item()) == 0:
+                inv = mixed.cholesky_inverse(f)
+            else:  # not positive definite in FP32: the mixed LU instead
+                f = mixed.lu_factor_tf32(ap, self.precision)
+                inv = mixed.lu_inverse(f, self.precision)
+            res = _Resident(ap, factor=f, inverse=inv, split=mixed.split_matrix(ap))
+            self._publish(req.op_id, "chol_mixed", req.n, res)
+        ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
+                            inner_max_steps=5, restart=8, factor=res.factor,
+                            inverse=res.inverse, split=res.split, precision=self.precision,
+                            arith="auto", fallback=True)
+        x = ir.x[:, : req.n].contiguous()
+        return Completion(req.rid, x, max(ir.berr), "chol_mixed", ir.fallback, reused)
+
     def _run_qr_mixed(self, req: Request) -> Completion:
         res = self._acquire(req.op_id)
         reused = res is not None
@@ -516,6 +550,8 @@ class SolveServer:
             jobs.append((self._run_small, groups["lu_small"]))
         for r in groups["lu_mixed"]:
             jobs.append((lambda rs: [self._run_mixed(rs[0])], [r]))
+        for r in groups["chol_mixed"]:
+            jobs.append((lambda rs: [self._run_chol_mixed(rs[0])], [r]))
         for r in groups["qr_mixed"]:
             jobs.append((lambda rs: [self._run_qr_mixed(rs[0])], [r]))
         for route in ("lu_f64", "chol_f64", "qr_f64"):

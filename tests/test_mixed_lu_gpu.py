@@ -242,3 +242,54 @@ def test_gmres_ir_precision_ladder(dev, cond):
     x = res.x.cpu().numpy()
     be = dense.backward_errors_exact(a, x, b)
     assert (be <= 1e-12 * (1 + 1e-4)).all(), be
+
+
+def spd(n, seed):
+    g = np.random.default_rng(seed).standard_normal((n, n))
+    return g @ g.T / n + 1e-2 * np.eye(n)
+
+
+@pytest.mark.parametrize("n", [64, 260, 1000, 2048])
+def test_cholesky_factor_tf32(dev, n):
+    """FP32 Cholesky with 3xTF32 tensor-core updates (lxgb_potrf_f32_tc) in the
+    mixed-LU form: L'U' = A to FP32 level, no interchanges, A read from its
+    upper triangle (the lower triangle is ignored), and its inverses
+    (L'^{-1} by substitution, U'^{-1} = L'^{-T} D^{-2}) within n u |X||T|."""
+    a = spd(n, n)
+    a_upper = np.triu(a)                  # lower triangle absent: it is not read
+    f = mixed.cholesky_factor_tf32(torch.tensor(a_upper, device=dev))
+    assert int(f.info) == 0
+    assert np.array_equal(f.piv.cpu().numpy(), np.arange(n))
+    lu = f.lu.double().cpu().numpy()
+    l = np.tril(lu, -1) + np.eye(n)
+    u = np.triu(lu)
+    rel = np.linalg.norm(a - l @ u) / np.linalg.norm(a)
+    assert rel < 5e-5, rel
+    # U' = D^2 L'^T exactly as formed: U'_ij = L'_ji * U'_jj... within FP32 rounding
+    assert np.allclose(u, np.diag(np.diag(u)) @ l.T, rtol=1e-5, atol=0)
+    inv = mixed.cholesky_inverse(f)
+    linv = inv.linv.double().cpu().numpy()
+    uinv = inv.uinv.double().cpu().numpy()
+    assert np.all(np.triu(linv, 1) == 0) and np.all(np.tril(uinv, -1) == 0)
+    for x, t in ((linv, l), (uinv, u)):
+        scale = np.abs(x) @ np.abs(t)
+        err = np.abs(x @ t - np.eye(n))
+        assert np.max(err[scale > 0] / scale[scale > 0]) < n * 2.0 ** -21
+
+
+def test_cholesky_factor_tf32_gmres_ir_and_indefinite(dev):
+    n = 1500 - 1500 % 4
+    a = spd(n, 3)
+    b = np.random.default_rng(4).standard_normal((5, n))
+    at = torch.tensor(a, device=dev)
+    f = mixed.cholesky_factor_tf32(at)
+    inv = mixed.cholesky_inverse(f)
+    res = mixed.gmres_ir(at, torch.tensor(b, device=dev), tol=1e-12, factor=f, inverse=inv,
+                         precision="3xtf32", arith="auto", fallback=True)
+    assert res.converged and not res.fallback, (res.outer, res.berr)
+    be = dense.backward_errors_exact(a, res.x.cpu().numpy(), b)
+    assert (be <= 1e-12 * (1 + 1e-4)).all(), be
+    # not positive definite: the first non-positive pivot is reported
+    m = -np.eye(128)
+    fm = mixed.cholesky_factor_tf32(torch.tensor(m, device=dev))
+    assert int(fm.info) == 1

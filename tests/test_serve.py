@@ -16,10 +16,13 @@ def req(rid, kind, n, k=1, op=None, arrival=0.0, with_a=True):
 
 def test_routes():
     assert serve.route_of("cholesky", 1024, "mixed") == "chol_ragged"
-    assert serve.route_of("cholesky", 1025, "mixed") == "lu_mixed"
+    assert serve.route_of("cholesky", 1025, "mixed") == "chol_mixed"
     assert serve.route_of("cholesky", 1025, "fp64") == "chol_f64"
     assert serve.route_of("qr", 100, "mixed") == "qr_f64"   # QR requests are served by QR
-    assert serve.route_of("qr", 169, "mixed") == "qr_mixed"
+    assert serve.route_of("qr", 169, "mixed") == "qr_f64"     # FP64 is faster below 512
+    assert serve.route_of("qr", 512, "mixed") == "qr_mixed"
+    assert serve.route_of("lu", 511, "mixed") == "lu_f64"
+    assert serve.route_of("lu", 512, "mixed") == "lu_mixed"
     assert serve.route_of("qr", 4096, "fp64") == "qr_f64"
     assert serve.route_of("lu", 100, "mixed") == "lu_small"
     assert serve.route_of("lu", 169, "fp64") == "lu_f64"
@@ -78,7 +81,7 @@ def test_synthetic_mix_shapes():
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["mixed", "fp64"])
 def test_serve_mix_backward_error_and_batch_independence(dev, mode):
-    reqs = serve.synthetic_requests(40, seed=3, nmax=700)
+    reqs = serve.synthetic_requests(40, seed=3, nmax=1400)   # every route up to chol_mixed
     srv = serve.SolveServer(dev, mode=mode)
     out = srv.run(reqs, realtime=False)
     assert len(out) == len(reqs)
