@@ -576,9 +576,9 @@ int lxgb_getrs_f32(int32_t n, int32_t nrhs, const float* lu, const int32_t* piv,
                    const double* b, double* x, void* stream);
 
 /* Inverse factors of a factor from lxgb_getrf_f32_tc: linv = L^{-1} (unit
- * lower, zeros above the diagonal) and uinv = U^{-1} (zeros below; uinv may
- * be NULL, then only L^{-1} is formed), both row-major n×n FP32, and perm with
- * (P b)_i = b[perm[i]].  Off-diagonal
+ * lower, zeros above the diagonal) and uinv = U^{-1} (zeros below; either one
+ * may be NULL, then only the other is formed), both row-major n×n FP32, and
+ * perm with (P b)_i = b[perm[i]].  Off-diagonal
  * updates on the tensor cores: precision 0 TF32, 1 3xTF32.  n <= 25600,
  * n % 4 == 0, lu 16-byte and work 256-byte aligned, work_bytes >=
  * lxgb_lu32_inverse_workspace_size.  *err is set if a tensor-core pipeline

@@ -405,7 +405,8 @@ extern "C" int lxgb_lu32_inverse(int32_t n, const float* lu, const int32_t* piv,
   LXGB_REQUIRE(n >= 0, "lu32_inverse: negative size");
   if (n == 0) return LXGB_SUCCESSFUL;
   LXGB_REQUIRE(n <= kPermMaxN, "lu32_inverse: n above 25600");
-  LXGB_REQUIRE(lu && piv && linv && perm && err && work, "lu32_inverse: null pointer");
+  LXGB_REQUIRE(lu && piv && (linv || uinv) && perm && err && work,
+               "lu32_inverse: null pointer");
   LXGB_REQUIRE((n % 4) == 0, "lu32_inverse: n must be a multiple of 4 (16-byte TMA rows)");
   LXGB_REQUIRE((((uintptr_t)lu) & 15) == 0 && (((uintptr_t)work) & 255) == 0,
                "lu32_inverse: lu must be 16-byte and work 256-byte aligned");
@@ -419,7 +420,7 @@ extern "C" int lxgb_lu32_inverse(int32_t n, const float* lu, const int32_t* piv,
                 "lu32_inverse: set smem");
   perm_from_swaps_kernel<<<1, 1024, psmem, st>>>(n, piv, perm);
   const unsigned idg = (unsigned)(n < 4096 ? n : 4096);
-  set_identity_f32_kernel<<<idg, 256, 0, st>>>(n, linv);
+  if (linv) set_identity_f32_kernel<<<idg, 256, 0, st>>>(n, linv);
   if (uinv) set_identity_f32_kernel<<<idg, 256, 0, st>>>(n, uinv);
   const int64_t blk = blk_bytes(n);
   char* wb = reinterpret_cast<char*>(work) + 256;
@@ -430,8 +431,9 @@ extern "C" int lxgb_lu32_inverse(int32_t n, const float* lu, const int32_t* piv,
   float* bl = reinterpret_cast<float*>(wb + 4 * blk);
   const bool split = precision == 1;
   // L^{-1}: top to bottom.  Row block j of W = L^{-1} has nonzeros in
-  // columns < j0 + nb only.
-  for (int j0 = 0; j0 < n; j0 += kInvNB) {
+  // columns < j0 + nb only.  (Skipped when linv is NULL: the square QR needs
+  // only R^{-1}.)
+  for (int j0 = 0; linv && j0 < n; j0 += kInvNB) {
     const int nb = min(kInvNB, n - j0);
     const int ncols = j0 + nb;
     inv_diag_kernel<true><<<(unsigned)((ncols + kInvCols - 1) / kInvCols), kInvCols, 0, st>>>(

@@ -561,11 +561,29 @@ def qr_factor_tf32(a: torch.Tensor) -> QR32:
     # square FP32 array with identity pivots (its lower triangle is ignored)
     if n % 4:
         return QR32(h, tau, t, rt, None)  # 16-byte TMA rows: FP64 triangular solves instead
-    r_sq = h[:, :n].t().contiguous()
-    piv = torch.arange(n, dtype=torch.int32, device=dev)
-    inv = lu_inverse(LU32(r_sq, piv, torch.zeros(1, dtype=torch.int32, device=dev)), "3xtf32")
-    inv = InverseLU32(inv.uinv.t().contiguous(), inv.uinv, inv.perm)
+    uinv, perm = _upper_inverse(h[:, :n].t().contiguous())
+    inv = InverseLU32(uinv.t().contiguous(), uinv, perm)
     return QR32(h, tau, t, rt, inv)
+
+
+def _upper_inverse(r_sq: torch.Tensor):
+    """(R^{-1}, identity perm) for R in the upper triangle of a square FP32
+    array (its lower triangle holds Householder vectors and is not read):
+    lxgb_lu32_inverse with linv NULL, 3xTF32 off-diagonal updates."""
+    n = r_sq.shape[0]
+    dev = r_sq.device
+    piv = torch.arange(n, dtype=torch.int32, device=dev)
+    uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, 1))
+    work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
+    _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(r_sq), _ffi.ptr(piv), None, _ffi.ptr(uinv),
+              _ffi.ptr(perm), 1, _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8,
+              _ffi.stream_handle(dev))
+    if int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
+    return uinv, perm
 
 
 def _gemv_df(split: SplitMatrix, x: torch.Tensor, b: torch.Tensor | None) -> torch.Tensor:
@@ -677,9 +695,8 @@ def qr_square_tf32(a: torch.Tensor) -> SquareQR32:
     del work, t, tau
     r_sq = h.t().contiguous()  # R on and above the diagonal
     del h
-    piv = torch.arange(n, dtype=torch.int32, device=dev)
-    inv = lu_inverse(LU32(r_sq, piv, torch.zeros(1, dtype=torch.int32, device=dev)), "3xtf32")
-    return SquareQR32(q.t().contiguous(), inv.uinv)
+    uinv, _ = _upper_inverse(r_sq)
+    return SquareQR32(q.t().contiguous(), uinv)
 
 
 class QRPreconditioner(_BlockOperator):
