@@ -407,9 +407,12 @@ typedef enum lxgb_operator_kind {
   LXGB_OP_POISSON5 = 1,
   LXGB_OP_SPLIT_DF = 2,  /* A = hi + lo (FP32 pair, row stride lda) applied in
                             double-float arithmetic, as lxgb_gemv_df mode 1 */
-  LXGB_OP_LU32_INV = 3   /* M = U^{-1} L^{-1} P from lxgb_lu32_inverse (hi =
+  LXGB_OP_LU32_INV = 3,  /* M = U^{-1} L^{-1} P from lxgb_lu32_inverse (hi =
                             L^{-1}, lo = U^{-1}, perm), as lxgb_lu32_apply
                             mode 1: the GMRES-IR preconditioner */
+  LXGB_OP_QR32 = 4       /* M = R^{-1} Qᵀ of a square FP32 QR (hi = Qᵀ, lo =
+                            R^{-1}, both n×n FP32), as lxgb_qr32_apply mode
+                            1: the GMRES-IR preconditioner of a QR solve */
 } lxgb_operator_kind;
 
 typedef struct lxgb_linear_operator {
@@ -420,8 +423,8 @@ typedef struct lxgb_linear_operator {
   int64_t lda;           /* LXGB_OP_DENSE, LXGB_OP_SPLIT_DF */
   int64_t nx, ny;        /* LXGB_OP_POISSON5 */
   double scale;          /* factor applied to the operator (1.0: as given) */
-  const float* hi;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV */
-  const float* lo;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV */
+  const float* hi;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV, LXGB_OP_QR32 */
+  const float* lo;       /* LXGB_OP_SPLIT_DF, LXGB_OP_LU32_INV, LXGB_OP_QR32 */
   const int32_t* perm;   /* LXGB_OP_LU32_INV */
 } lxgb_linear_operator;
 

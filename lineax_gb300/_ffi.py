@@ -184,7 +184,7 @@ class LinearOperatorDesc(ctypes.Structure):
                 ("hi", c_p), ("lo", c_p), ("perm", c_p)]
 
 
-OP_DENSE, OP_POISSON5, OP_SPLIT_DF, OP_LU32_INV = 0, 1, 2, 3
+OP_DENSE, OP_POISSON5, OP_SPLIT_DF, OP_LU32_INV, OP_QR32 = 0, 1, 2, 3, 4
 
 
 def lib_path() -> pathlib.Path:

@@ -1010,7 +1010,9 @@ __global__ void scale_kernel(int64_t total, double s, double* __restrict__ y) {
 static int64_t apply_scratch_bytes(int k, int64_t n) {
   const int64_t a = lxgb_gemv_df_workspace_size((int32_t)n, k);
   const int64_t b = lxgb_lu32_apply_workspace_size((int32_t)n, k);
-  return al256((int64_t)k * n * 8) + al256(a > b ? a : b);
+  const int64_t c = lxgb_qr32_apply_workspace_size((int32_t)n, k);
+  const int64_t m = a > b ? a : b;
+  return al256((int64_t)k * n * 8) + al256(m > c ? m : c);
 }
 
 // y = op(x) for k vectors; x_c at x + c*ldx, y contiguous.  `tmp` holds
@@ -1033,7 +1035,10 @@ static int apply_op(const lxgb_linear_operator& op, int k, int64_t n, const doub
       x = tmp;
     }
     if (op.kind == LXGB_OP_POISSON5) return lxgb_poisson5_f64(op.nx, op.ny, k, op.scale, x, y, st);
-    rc = lxgb_lu32_apply((int32_t)n, k, op.hi, op.lo, op.perm, 1, x, y, scratch, sbytes, st);
+    if (op.kind == LXGB_OP_QR32)
+      rc = lxgb_qr32_apply((int32_t)n, k, op.hi, op.lo, 1, x, y, scratch, sbytes, st);
+    else
+      rc = lxgb_lu32_apply((int32_t)n, k, op.hi, op.lo, op.perm, 1, x, y, scratch, sbytes, st);
   }
   if (!rc && op.scale != 1.0) {
     const int64_t total = (int64_t)k * n;
@@ -1060,9 +1065,12 @@ static int check_op(const lxgb_linear_operator* op, int64_t n, const char* who) 
     }
     return LXGB_SUCCESSFUL;
   }
-  if (op->kind == LXGB_OP_SPLIT_DF || op->kind == LXGB_OP_LU32_INV) {
+  if (op->kind == LXGB_OP_SPLIT_DF || op->kind == LXGB_OP_LU32_INV ||
+      op->kind == LXGB_OP_QR32) {
     const bool ok = op->hi && n < (1LL << 31) &&
-                    (op->kind == LXGB_OP_SPLIT_DF ? op->lda >= n : (op->lo && op->perm));
+                    (op->kind == LXGB_OP_SPLIT_DF ? op->lda >= n
+                     : op->kind == LXGB_OP_QR32   ? op->lo != nullptr
+                                                  : (op->lo && op->perm));
     if (!ok) {
       set_last_error("%s: FP32 operator needs its factor arrays (and lda >= n)", who);
       return LXGB_INVALID_ARG;

@@ -363,10 +363,10 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     tried.  stop_on_stall (default: fallback) ends the loop at the first stall
     of the GMRES tier.
 
-    device_loop (arith "auto" with the LU preconditioner) runs the whole
-    refinement loop as one call of lxgb_gmres_ir_run — the same kernels in the
-    same order, with the loop decisions taken on the device — and returns to
-    the host once, at the end."""
+    device_loop (arith "auto", with the LU or the QR preconditioner) runs the
+    whole refinement loop as one call of lxgb_gmres_ir_run — the same kernels
+    in the same order, with the loop decisions taken on the device — and
+    returns to the host once, at the end."""
     a64 = as_device_f64(a)
     b64 = as_device_f64(b)
     if b64.ndim == 1:
@@ -403,12 +403,12 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
     if split is None:
         split = split_matrix(a64)
     outer_op = SplitMatrixOperator(split, "df")
-    if device_loop and arith == "auto" and qr is None:
-        if inverse is None:
+    if device_loop and arith == "auto":
+        if qr is None and inverse is None:
             inverse = lu_inverse(factor, precision)
         return _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart,
                                 stagnation_iters, max_outer, inner_max_steps, fallback,
-                                stop_on_stall)
+                                stop_on_stall, qr=qr)
     tiers = ["ir", "df"] if arith == "auto" else [arith]
     tier = 0
     made = {"inverse": inverse}
@@ -468,17 +468,23 @@ def gmres_ir(a: torch.Tensor, b: torch.Tensor, *, tol: float = 1e-12, inner_rtol
 
 
 def _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart, stagnation_iters,
-                     max_outer, inner_max_steps, fallback, stop_on_stall) -> IRResult:
-    """gmres_ir's "auto" loop as one lxgb_gmres_ir_run call."""
+                     max_outer, inner_max_steps, fallback, stop_on_stall,
+                     qr: "SquareQR32 | None" = None) -> IRResult:
+    """gmres_ir's "auto" loop as one lxgb_gmres_ir_run call, preconditioned by
+    the LU inverses (LXGB_OP_LU32_INV) or by R^{-1} Qᵀ (LXGB_OP_QR32)."""
     import ctypes
 
     k, n = b64.shape
     dev = b64.device
     op = _ffi.LinearOperatorDesc(kind=_ffi.OP_SPLIT_DF, n=n, lda=n, scale=1.0,
                                  hi=split.hi.data_ptr(), lo=split.lo.data_ptr())
-    pre = _ffi.LinearOperatorDesc(kind=_ffi.OP_LU32_INV, n=n, scale=1.0,
-                                  hi=inverse.linv.data_ptr(), lo=inverse.uinv.data_ptr(),
-                                  perm=inverse.perm.data_ptr())
+    if qr is not None:
+        pre = _ffi.LinearOperatorDesc(kind=_ffi.OP_QR32, n=n, scale=1.0,
+                                      hi=qr.qt.data_ptr(), lo=qr.rinv.data_ptr())
+    else:
+        pre = _ffi.LinearOperatorDesc(kind=_ffi.OP_LU32_INV, n=n, scale=1.0,
+                                      hi=inverse.linv.data_ptr(), lo=inverse.uinv.data_ptr(),
+                                      perm=inverse.perm.data_ptr())
     anorm = norm_inf(a64).reshape(1)
     x = torch.empty_like(b64)
     berr = torch.empty(k, dtype=torch.float64, device=dev)
@@ -498,7 +504,7 @@ def _gmres_ir_device(a64, b64, split, inverse, tol, inner_rtol, restart, stagnat
     if fallback and not converged:
         outer_op = SplitMatrixOperator(split, "df")
         return _fp64_fallback(a64, b64, outer_op, float(anorm.item()), _kmax(b64).cpu(), tol,
-                              outer, [int(reached_gmres)] * outer)
+                              outer, [int(reached_gmres)] * outer, use_qr=qr is not None)
     return IRResult(x, berr_h, outer, [int(reached_gmres)] * outer, converged, inverse=inverse)
 
 

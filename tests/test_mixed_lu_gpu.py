@@ -207,6 +207,28 @@ def test_gmres_ir_single_call_equals_host_loop(dev, n, cond, precision, max_oute
     assert (max(host.inner_steps) > 0) == (max(devl.inner_steps) > 0)
 
 
+@pytest.mark.parametrize("n", [256, 1000])
+def test_gmres_ir_qr_single_call_equals_host_loop(dev, n):
+    """The QR-preconditioned refinement (M = R^{-1} Qᵀ of the square TF32 QR,
+    LXGB_OP_QR32) in one lxgb_gmres_ir_run call equals the host loop bit for
+    bit, and reaches the FP64 backward error."""
+    g = np.random.default_rng(n).standard_normal((n, n))
+    a_h = g / np.sqrt(n) + np.eye(n)
+    a = torch.tensor(a_h, device=dev)
+    b_h = np.random.default_rng(n + 1).standard_normal((2, n))
+    b = torch.tensor(b_h, device=dev)
+    qr = mixed.qr_square_tf32(a)
+    sp = mixed.split_matrix(a)
+    kw = dict(tol=1e-12, restart=8, inner_max_steps=5, max_outer=20, split=sp, qr=qr,
+              arith="auto", fallback=False)
+    host = mixed.gmres_ir(a, b, device_loop=False, **kw)
+    devl = mixed.gmres_ir(a, b, device_loop=True, **kw)
+    assert devl.converged and torch.equal(host.x, devl.x)
+    assert host.outer == devl.outer and host.berr == devl.berr
+    be = dense.backward_errors_exact(a_h, devl.x.cpu().numpy(), b_h)
+    assert (be <= 1e-12 * (1 + 1e-4)).all(), be
+
+
 @pytest.mark.parametrize("n", [256, 1024, 2048])
 def test_bf16_lu_factorisation_residual(dev, n):
     """BF16 tensor-core updates (8-bit significands, FP32 accumulation): the
