@@ -44,7 +44,18 @@ PRECISIONS = {"tf32": 0, "3xtf32": 1, "bf16": 2}
 LADDER = ("bf16", "tf32", "3xtf32")
 
 
-def lu_factor_tf32(a: torch.Tensor, precision: str = "tf32") -> LU32:
+def _pipeline_err(err: torch.Tensor | None, dev) -> tuple:
+    """(err tensor, whether to check it now): callers that pass their own
+    device flag read it later themselves (one synchronisation per request
+    instead of one per stage, so the host keeps enqueueing while the GPU
+    works)."""
+    if err is None:
+        return torch.zeros(1, dtype=torch.int32, device=dev), True
+    return err, False
+
+
+def lu_factor_tf32(a: torch.Tensor, precision: str = "tf32",
+                   err: torch.Tensor | None = None) -> LU32:
     """FP32 LU with partial pivoting and tensor-core trailing updates:
     precision "bf16" (BF16 products, FP32 accumulation), "tf32" (one TF32
     product) or "3xtf32" (FP32-level accuracy)."""
@@ -58,18 +69,18 @@ def lu_factor_tf32(a: torch.Tensor, precision: str = "tf32") -> LU32:
     lu = torch.empty((n, n), dtype=torch.float32, device=dev)
     piv = torch.empty(n, dtype=torch.int32, device=dev)
     info = torch.empty(1, dtype=torch.int32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     prec = PRECISIONS[precision]
     wbytes = int(_ffi.load().lxgb_getrf_f32_tc_workspace_size(n, prec))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     _ffi.call("lxgb_getrf_f32_tc", n, _ffi.ptr(a64), _ffi.ptr(lu), _ffi.ptr(piv), _ffi.ptr(info),
               prec, _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8, _ffi.stream_handle(dev))
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the LU update")
     return LU32(lu, piv, info)
 
 
-def cholesky_factor_tf32(a: torch.Tensor) -> LU32:
+def cholesky_factor_tf32(a: torch.Tensor, err: torch.Tensor | None = None) -> LU32:
     """FP32 Cholesky A = L Lᵀ with 3xTF32 tensor-core updates
     (lxgb_potrf_f32_tc; A read from its upper triangle), returned in the
     unit-lower / upper form of lu_factor_tf32 (L' = L D⁻¹, U' = D Lᵀ, no
@@ -86,19 +97,19 @@ def cholesky_factor_tf32(a: torch.Tensor) -> LU32:
     lu = torch.empty((n, n), dtype=torch.float32, device=dev)
     piv = torch.empty(n, dtype=torch.int32, device=dev)
     info = torch.empty(1, dtype=torch.int32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     wbytes = int(_ffi.load().lxgb_potrf_f32_tc_workspace_size(n))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     s = _ffi.stream_handle(dev)
     _ffi.call("lxgb_potrf_f32_tc", n, _ffi.ptr(a64), _ffi.ptr(l), _ffi.ptr(info), _ffi.ptr(err),
               _ffi.ptr(work), work.numel() * 8, s)
     _ffi.call("lxgb_chol32_to_lu32", n, _ffi.ptr(l), _ffi.ptr(lu), _ffi.ptr(piv), s)
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the Cholesky update")
     return LU32(lu, piv, info)
 
 
-def cholesky_inverse(factor: LU32) -> InverseLU32:
+def cholesky_inverse(factor: LU32, err: torch.Tensor | None = None) -> InverseLU32:
     """Triangular inverses of a factor from cholesky_factor_tf32: L'⁻¹ by the
     tensor-core substitution of lu_inverse, U'⁻¹ = L'⁻ᵀ D⁻² by a transposing
     copy (no second substitution)."""
@@ -108,14 +119,14 @@ def cholesky_inverse(factor: LU32) -> InverseLU32:
     linv = torch.empty((n, n), dtype=torch.float32, device=dev)
     uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
     perm = torch.empty(n, dtype=torch.int32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, 1))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     s = _ffi.stream_handle(dev)
     _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(lu), _ffi.ptr(factor.piv), _ffi.ptr(linv), None,
               _ffi.ptr(perm), 1, _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8, s)
     _ffi.call("lxgb_chol32_uinv", n, _ffi.ptr(lu), _ffi.ptr(linv), _ffi.ptr(uinv), s)
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
     return InverseLU32(linv, uinv, perm)
 
@@ -163,7 +174,8 @@ class InverseLU32:
     perm: torch.Tensor  # (P b)_i = b[perm[i]]
 
 
-def lu_inverse(factor: LU32, precision: str = "3xtf32") -> InverseLU32:
+def lu_inverse(factor: LU32, precision: str = "3xtf32",
+               err: torch.Tensor | None = None) -> InverseLU32:
     """Triangular inverses of an FP32 LU, off-diagonal blocks on the tensor cores."""
     lu = factor.lu
     n = lu.shape[0]
@@ -171,14 +183,14 @@ def lu_inverse(factor: LU32, precision: str = "3xtf32") -> InverseLU32:
     linv = torch.empty((n, n), dtype=torch.float32, device=dev)
     uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
     perm = torch.empty(n, dtype=torch.int32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     prec = min(PRECISIONS[precision], 1)  # a BF16 factor's inverses use TF32 updates
     wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, prec))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(lu), _ffi.ptr(factor.piv), _ffi.ptr(linv),
               _ffi.ptr(uinv), _ffi.ptr(perm), prec, _ffi.ptr(err), _ffi.ptr(work),
               work.numel() * 8, _ffi.stream_handle(dev))
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
     return InverseLU32(linv, uinv, perm)
 
@@ -572,7 +584,7 @@ def qr_factor_tf32(a: torch.Tensor) -> QR32:
     return QR32(h, tau, t, rt, inv)
 
 
-def _upper_inverse(r_sq: torch.Tensor):
+def _upper_inverse(r_sq: torch.Tensor, err: torch.Tensor | None = None):
     """(R^{-1}, identity perm) for R in the upper triangle of a square FP32
     array (its lower triangle holds Householder vectors and is not read):
     lxgb_lu32_inverse with linv NULL, 3xTF32 off-diagonal updates."""
@@ -581,13 +593,13 @@ def _upper_inverse(r_sq: torch.Tensor):
     piv = torch.arange(n, dtype=torch.int32, device=dev)
     uinv = torch.empty((n, n), dtype=torch.float32, device=dev)
     perm = torch.empty(n, dtype=torch.int32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     wbytes = int(_ffi.load().lxgb_lu32_inverse_workspace_size(n, 1))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     _ffi.call("lxgb_lu32_inverse", n, _ffi.ptr(r_sq), _ffi.ptr(piv), None, _ffi.ptr(uinv),
               _ffi.ptr(perm), 1, _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8,
               _ffi.stream_handle(dev))
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the triangular inversion")
     return uinv, perm
 
@@ -676,7 +688,7 @@ class SquareQR32:
     rinv: torch.Tensor  # R^{-1}, n×n FP32 (zeros below the diagonal)
 
 
-def qr_square_tf32(a: torch.Tensor) -> SquareQR32:
+def qr_square_tf32(a: torch.Tensor, err: torch.Tensor | None = None) -> SquareQR32:
     """A = Q R for a square A (n % 4 == 0): FP32 Householder QR with tcgen05
     TF32 updates that also forms Q (lxgb_geqrf_f32_tc_q), and R^{-1} by the
     tensor-core triangular inversion (3xTF32)."""
@@ -690,18 +702,18 @@ def qr_square_tf32(a: torch.Tensor) -> SquareQR32:
     tau = torch.empty(n, dtype=torch.float32, device=dev)
     t = torch.empty(max(1, int(lib.lxgb_geqrf_t_elems(n))), dtype=torch.float32, device=dev)
     q = torch.empty((n, n), dtype=torch.float32, device=dev)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err, check = _pipeline_err(err, dev)
     wbytes = int(lib.lxgb_geqrf_f32_tc_q_workspace_size(n, n))
     work = torch.empty(wbytes // 8 + 1, dtype=torch.float64, device=dev)
     _ffi.call("lxgb_geqrf_f32_tc_q", n, n, _ffi.ptr(a64), _ffi.ptr(h), _ffi.ptr(tau), _ffi.ptr(t),
               _ffi.ptr(q), _ffi.ptr(err), _ffi.ptr(work), work.numel() * 8,
               _ffi.stream_handle(dev))
-    if int(err.item()) != 0:
+    if check and int(err.item()) != 0:
         raise RuntimeError("tensor-core pipeline timed out during the QR update")
     del work, t, tau
     r_sq = h.t().contiguous()  # R on and above the diagonal
     del h
-    uinv, _ = _upper_inverse(r_sq)
+    uinv, _ = _upper_inverse(r_sq, None if check else err)
     return SquareQR32(q.t().contiguous(), uinv)
 
 

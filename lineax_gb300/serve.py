@@ -246,6 +246,13 @@ class Scheduler:
                 self.resident_total += int(nbytes)
 
 
+def _check_pipeline(err) -> None:
+    """Raise if a tensor-core pipeline wait of the request's factorisation
+    gave up (the flag is read after the refinement has synchronised)."""
+    if err is not None and int(err.item()) != 0:
+        raise RuntimeError("tensor-core pipeline timed out while factoring a request")
+
+
 def _pad_identity(a: torch.Tensor, n_to: int) -> torch.Tensor:
     n = a.shape[0]
     if n == n_to:
@@ -464,16 +471,21 @@ class SolveServer:
         res = self._acquire(req.op_id)
         reused = res is not None
         n4 = (req.n + 3) // 4 * 4
+        err = None
         if res is None:
+            # one pipeline flag for the request, read after the refinement's
+            # own synchronisation: the host keeps enqueueing meanwhile
+            err = torch.zeros(1, dtype=torch.int32, device=self.device)
             ap = _pad_identity(self._matrix(req), n4)
-            f = mixed.lu_factor_tf32(ap, self.precision)
-            res = _Resident(ap, factor=f, inverse=mixed.lu_inverse(f, self.precision),
+            f = mixed.lu_factor_tf32(ap, self.precision, err=err)
+            res = _Resident(ap, factor=f, inverse=mixed.lu_inverse(f, self.precision, err=err),
                             split=mixed.split_matrix(ap))
             self._publish(req.op_id, "lu_mixed", req.n, res)
         ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
                             inner_max_steps=5, restart=8, factor=res.factor,
                             inverse=res.inverse, split=res.split, precision=self.precision,
                             arith="auto", fallback=True)
+        _check_pipeline(err)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "lu_mixed", ir.fallback, reused)
 
@@ -481,20 +493,23 @@ class SolveServer:
         res = self._acquire(req.op_id)
         reused = res is not None
         n4 = (req.n + 3) // 4 * 4
+        err = None
         if res is None:
+            err = torch.zeros(1, dtype=torch.int32, device=self.device)
             ap = _pad_identity(self._matrix(req), n4)
-            f = mixed.cholesky_factor_tf32(ap)
+            f = mixed.cholesky_factor_tf32(ap, err=err)
             if int(f.info.item()) == 0:
-                inv = mixed.cholesky_inverse(f)
+                inv = mixed.cholesky_inverse(f, err=err)
             else:  # not positive definite in FP32: the mixed LU instead
-                f = mixed.lu_factor_tf32(ap, self.precision)
-                inv = mixed.lu_inverse(f, self.precision)
+                f = mixed.lu_factor_tf32(ap, self.precision, err=err)
+                inv = mixed.lu_inverse(f, self.precision, err=err)
             res = _Resident(ap, factor=f, inverse=inv, split=mixed.split_matrix(ap))
             self._publish(req.op_id, "chol_mixed", req.n, res)
         ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
                             inner_max_steps=5, restart=8, factor=res.factor,
                             inverse=res.inverse, split=res.split, precision=self.precision,
                             arith="auto", fallback=True)
+        _check_pipeline(err)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "chol_mixed", ir.fallback, reused)
 
@@ -502,13 +517,16 @@ class SolveServer:
         res = self._acquire(req.op_id)
         reused = res is not None
         n4 = (req.n + 3) // 4 * 4
+        err = None
         if res is None:
+            err = torch.zeros(1, dtype=torch.int32, device=self.device)
             ap = _pad_identity(self._matrix(req), n4)
-            res = _Resident(ap, qr=mixed.qr_square_tf32(ap), split=mixed.split_matrix(ap))
+            res = _Resident(ap, qr=mixed.qr_square_tf32(ap, err=err), split=mixed.split_matrix(ap))
             self._publish(req.op_id, "qr_mixed", req.n, res)
         ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
                             inner_max_steps=5, restart=8, split=res.split, qr=res.qr,
                             arith="auto", fallback=True)
+        _check_pipeline(err)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "qr_mixed", ir.fallback, reused)
 
@@ -590,6 +608,12 @@ class SolveServer:
         worker threads with one CUDA stream each.  Returns the completions in
         request-id order with finish times and latencies."""
         for r in sorted(requests, key=lambda q: q.arrival):
+            # A request carrying its matrix registers the client's copy when
+            # it is sent, so a later request on the same operator finds it
+            # even if it executes first (its worker may run ahead of the
+            # defining request's worker).
+            if r.a is not None:
+                self.registry.setdefault(r.op_id, r.a)
             self.sched.submit(r)
         arrival = {r.rid: r.arrival for r in requests}
         done = {}
