@@ -682,46 +682,55 @@ __device__ __noinline__ int mx_factor_large(const double* __restrict__ A, float*
 }
 
 // --- solves: (Uᵀ U) D = D for the live vectors of a chunk ------------------
-// U row stride ld (shared or global memory); D[c*n + i] in shared memory;
+// U row stride ld (shared or global memory); D[i*kMxKc + c] in shared memory;
 // rd = 1/diag(U).  The warp solving a 32×32 diagonal block loads its column
 // (forward) or row (backward) of the block into registers first, so the
 // sequential steps only exchange values by shuffles; the off-diagonal
 // updates take one matrix row or column per thread for all NC vectors.
 // Off-diagonal updates of the blocked substitution for the first W vectors
 // of D (the rest are padding): rows below block [r0, r0+rn) in the forward
-// pass, rows above it in the backward pass; one matrix row per thread.
+// pass, rows above it in the backward pass; one matrix row per thread.  D is
+// row-major with kMxKc vectors per row (16-byte aligned rows), so the solved
+// values of step t reach every thread as W/4 broadcast 16-byte loads.
+template <int W>
+__device__ __forceinline__ void mx_rows_fma(float (&v)[W], float u, const float* drow) {
+  const float4* d4 = reinterpret_cast<const float4*>(drow);
+#pragma unroll
+  for (int q = 0; q < W / 4; ++q) {
+    const float4 d = d4[q];
+    v[4 * q + 0] = fmaf(-u, d.x, v[4 * q + 0]);
+    v[4 * q + 1] = fmaf(-u, d.y, v[4 * q + 1]);
+    v[4 * q + 2] = fmaf(-u, d.z, v[4 * q + 2]);
+    v[4 * q + 3] = fmaf(-u, d.w, v[4 * q + 3]);
+  }
+}
+
 template <int W>
 __device__ __forceinline__ void mx_solve_rows_below(const float* U, int ld, int n, int r0, int rn,
                                                     float* D) {
+  static_assert(W % 4 == 0, "vectors go in groups of four");
   for (int i = r0 + rn + threadIdx.x; i < n; i += blockDim.x) {
     float v[W];
 #pragma unroll
-    for (int c = 0; c < W; ++c) v[c] = D[c * n + i];
-    for (int t = 0; t < rn; ++t) {
-      const float u = U[(r0 + t) * ld + i];
+    for (int c = 0; c < W; ++c) v[c] = D[i * kMxKc + c];
+    for (int t = 0; t < rn; ++t) mx_rows_fma<W>(v, U[(r0 + t) * ld + i], D + (r0 + t) * kMxKc);
 #pragma unroll
-      for (int c = 0; c < W; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < W; ++c) D[c * n + i] = v[c];
+    for (int c = 0; c < W; ++c) D[i * kMxKc + c] = v[c];
   }
 }
 
 template <int W>
 __device__ __forceinline__ void mx_solve_rows_above(const float* U, int ld, int n, int r0, int rn,
                                                     float* D) {
+  static_assert(W % 4 == 0, "vectors go in groups of four");
   for (int i = threadIdx.x; i < r0; i += blockDim.x) {
     const float* rowp = U + i * ld + r0;
     float v[W];
 #pragma unroll
-    for (int c = 0; c < W; ++c) v[c] = D[c * n + i];
-    for (int t = 0; t < rn; ++t) {
-      const float u = rowp[t];
+    for (int c = 0; c < W; ++c) v[c] = D[i * kMxKc + c];
+    for (int t = 0; t < rn; ++t) mx_rows_fma<W>(v, rowp[t], D + (r0 + t) * kMxKc);
 #pragma unroll
-      for (int c = 0; c < W; ++c) v[c] = fmaf(-u, D[c * n + r0 + t], v[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < W; ++c) D[c * n + i] = v[c];
+    for (int c = 0; c < W; ++c) D[i * kMxKc + c] = v[c];
   }
 }
 
@@ -739,13 +748,13 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
 #pragma unroll
       for (int t = 0; t < 32; ++t) col[t] = (t < lane && lane < rn) ? U[(r0 + t) * ld + r0 + lane] : 0.0f;
       const float rdl = (lane < rn) ? rd[r0 + lane] : 0.0f;
-      float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
+      float v = (lane < rn) ? D[(r0 + lane) * kMxKc + c] : 0.0f;
 #pragma unroll
       for (int t = 0; t < 32; ++t) {  // lanes >= rn carry zeros, so all 32 steps run
         const float yt = __shfl_sync(0xffffffffu, v * rdl, t);
         v = (lane == t) ? yt : ((lane > t) ? fmaf(-col[t], yt, v) : v);
       }
-      if (lane < rn) D[c * n + r0 + lane] = v;
+      if (lane < rn) D[(r0 + lane) * kMxKc + c] = v;
     }
     __syncthreads();
     if (nc <= NC / 2)
@@ -762,13 +771,13 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
 #pragma unroll
       for (int t = 0; t < 32; ++t) row[t] = (t > lane && t < rn) ? U[(r0 + lane) * ld + r0 + t] : 0.0f;
       const float rdl = (lane < rn) ? rd[r0 + lane] : 0.0f;
-      float v = (lane < rn) ? D[c * n + r0 + lane] : 0.0f;
+      float v = (lane < rn) ? D[(r0 + lane) * kMxKc + c] : 0.0f;
 #pragma unroll
       for (int tt = 31; tt >= 0; --tt) {
         const float xt = __shfl_sync(0xffffffffu, v * rdl, tt);
         v = (lane == tt) ? xt : ((lane < tt) ? fmaf(-row[tt], xt, v) : v);
       }
-      if (lane < rn) D[c * n + r0 + lane] = v;
+      if (lane < rn) D[(r0 + lane) * kMxKc + c] = v;
     }
     __syncthreads();
     if (nc <= NC / 2)
@@ -779,7 +788,7 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
   }
 }
 
-// --- residual: D = fl32(B - A X) with X = XH + XL, FP64-accurate, no FP64 ops
+// --- residual: D = fl32(B - A X) with X = hi + lo (float2), FP64-accurate, no FP64 ops
 // A is split bitwise into hi+lo, hi*xh products made exact by an FMA
 // (TwoProd) and summed with TwoSum; ah*xl + al*xh, the product errors and the
 // summation errors go to a second FP32 accumulator.  b - Ax is formed in the
@@ -789,8 +798,8 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
 // and x = 0 there, so their residual is 0.
 template <int NC>
 __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, int nc,
-                              const double* __restrict__ B, const float* XH, const float* XL,
-                              float* D, MxSmem& sm) {
+                              const double* __restrict__ B, const float2* XV, float* D,
+                              MxSmem& sm) {
   static_assert(NC == 8, "the transposing reduction below is written for 8 vectors");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const int cl = lane >> 2;            // the vector this lane finishes (lanes 4c..4c+3)
@@ -831,19 +840,21 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
       splitw<8>(av, ah, al);
 #pragma unroll
       for (int u = 0; u < 8; ++u) rs += fabsf(ah[u]);   // ah = 0 past the row's end
-      // vectors 0..3, then 4..7 only when the chunk has more than four live
-      // ones (the rest are padding); per vector the terms go in j order
+      // vectors in pairs, a pair only when it holds a live one (the rest
+      // are padding); per vector the terms go in j order.  x is read as one
+      // 8-byte (hi, lo) pair per element.
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        if (h == 1 && nc <= 4) break;
+      for (int h = 0; h < 4; ++h) {
+        if (h > 0 && 2 * h >= nc) break;
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int j = j0 + lane + 32 * u;
           if (j < n) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int c = 4 * h + k;
-              const float xh = XH[c * n + j], xl = XL[c * n + j];
+            for (int k = 0; k < 2; ++k) {
+              const int c = 2 * h + k;
+              const float2 xv = XV[c * n + j];
+              const float xh = xv.x, xl = xv.y;
               const float p = ah[u] * xh;
               const float pe = fmaf(ah[u], xh, -p);
               float err;
@@ -909,7 +920,7 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
       float rh = bh, re;
       two_sum(rh, -S1, re);
       const float r = rh + ((bl - C1) + re);
-      D[cl * n + i] = r;
+      D[i * kMxKc + cl] = r;
       rmax = fmaxf(rmax, fabsf(r));
     }
   }
@@ -920,7 +931,7 @@ __device__ __noinline__ void mx_residual_t(const double* __restrict__ A, int n, 
 // x += d in double-float (TwoSum then Fast2Sum renormalisation) for live
 // vectors; per-warp max |x| into sm.red2[warp][1 + c].
 template <int NC>
-__device__ __noinline__ void mx_update_x(int n, const float* D, float* XH, float* XL, MxSmem& sm) {
+__device__ __noinline__ void mx_update_x(int n, const float* D, float2* XV, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float xm[NC];
 #pragma unroll
@@ -929,14 +940,14 @@ __device__ __noinline__ void mx_update_x(int n, const float* D, float* XH, float
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (!sm.done[c]) {
-        float s = XH[c * n + i], e;
-        two_sum(s, D[c * n + i], e);
-        const float t = XL[c * n + i] + e;
+        const float2 xv = XV[c * n + i];
+        float s = xv.x, e;
+        two_sum(s, D[i * kMxKc + c], e);
+        const float t = xv.y + e;
         const float h = s + t;
-        XH[c * n + i] = h;
-        XL[c * n + i] = t - (h - s);
+        XV[c * n + i] = make_float2(h, t - (h - s));
       }
-      xm[c] = fmaxf(xm[c], fabsf(XH[c * n + i]));
+      xm[c] = fmaxf(xm[c], fabsf(XV[c * n + i].x));
     }
   }
 #pragma unroll
@@ -960,7 +971,7 @@ __device__ __noinline__ void mx_update_x(int n, const float* D, float* XH, float
 template <int NC>
 __device__ void mx_refine(const float* F, int ld, int n, int nc, const double* __restrict__ A,
                           const double* __restrict__ B, double* __restrict__ X, float* D,
-                          float* XH, float* XL, double tol, int max_iter, bool& first_residual,
+                          float2* XV, double tol, int max_iter, bool& first_residual,
                           int& iters_out, bool& converged, MxSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   if (tid < kMxKc) { sm.done[tid] = tid >= nc; sm.berr[tid] = 0.0; }
@@ -972,9 +983,8 @@ __device__ void mx_refine(const float* F, int ld, int n, int nc, const double* _
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       const float v = (c < nc) ? to_f32(B[(int64_t)c * n + i]) : 0.0f;
-      D[c * n + i] = v;
-      XH[c * n + i] = 0.0f;
-      XL[c * n + i] = 0.0f;
+      D[i * kMxKc + c] = v;
+      XV[c * n + i] = make_float2(0.0f, 0.0f);
       bm[c] = fmaxf(bm[c], fabsf(v));
     }
   }
@@ -996,10 +1006,10 @@ __device__ void mx_refine(const float* F, int ld, int n, int nc, const double* _
   bool all_done = false;
   for (;;) {
     mx_solve_t<NC>(F, ld, n, nc, D, sm.rd, sm);
-    mx_update_x<NC>(n, D, XH, XL, sm);
+    mx_update_x<NC>(n, D, XV, sm);
     ++it;
     __syncthreads();
-    mx_residual_t<NC>(A, n, nc, B, XH, XL, D, sm);
+    mx_residual_t<NC>(A, n, nc, B, XV, D, sm);
     __syncthreads();
     if (tid == 0) {
       if (first_residual) {
@@ -1033,7 +1043,10 @@ __device__ void mx_refine(const float* F, int ld, int n, int nc, const double* _
   for (int i = tid; i < n; i += blockDim.x) {
 #pragma unroll
     for (int c = 0; c < NC; ++c)
-      if (c < nc) X[(int64_t)c * n + i] = (double)XH[c * n + i] + (double)XL[c * n + i];
+      if (c < nc) {
+        const float2 xv = XV[c * n + i];
+        X[(int64_t)c * n + i] = (double)xv.x + (double)xv.y;
+      }
   }
   iters_out = it;
   converged = all_done;
@@ -1148,10 +1161,11 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
     const int ld = small ? (n | 1) : ((n + 31) & ~31);
     const int ldmax = (max_n + 31) & ~31;
     float* F = small ? smem_mx : factor_ws + (int64_t)blockIdx.x * ldmax * ldmax;
-    float* vec = small ? smem_mx + n * ld : smem_mx;   // D | XH | XL, kMxKc*n each
+    // D (n rows of kMxKc floats) | x as (hi, lo) pairs (kMxKc*n float2),
+    // 16-byte aligned
+    float* vec = small ? smem_mx + ((n * ld + 3) & ~3) : smem_mx;
     float* D = vec;
-    float* XH = vec + kMxKc * n;
-    float* XL = vec + 2 * kMxKc * n;
+    float2* XV = reinterpret_cast<float2*>(vec + kMxKc * n);
     if (tid == 0) sm.flag = 0;
     const int fm = fmode ? fmode[s] : kFactorCompute;
     int rc;
@@ -1199,7 +1213,7 @@ posv_mixed_kernel(int64_t batch, int max_n, int max_nrhs, const int32_t* __restr
       double* X = x + b_off[s] + (int64_t)c0 * n;
       int it = 0;
       bool conv = true;
-      mx_refine<kMxKc>(F, ld, n, nc, A, B, X, D, XH, XL, tol, max_iter, first, it, conv, sm);
+      mx_refine<kMxKc>(F, ld, n, nc, A, B, X, D, XV, tol, max_iter, first, it, conv, sm);
       if (!conv) sys_info = -1;
       for (int c = 0; c < nc; ++c) sys_berr = fmax(sys_berr, sm.berr[c]);
       sys_iters = max(sys_iters, it);
@@ -1231,7 +1245,9 @@ static std::atomic<int> g_mx_tc{0};
 static size_t mixed_smem_bytes(int max_n, int max_nrhs, int small_max) {
   (void)max_nrhs;
   const int ns = max_n < small_max ? max_n : small_max;
-  const size_t small = (size_t)ns * (ns | 1) * sizeof(float) + (size_t)3 * kMxKc * ns * sizeof(float);
+  // + three floats: the vectors start on a 16-byte boundary after the factor
+  const size_t small =
+      (size_t)(ns * (ns | 1) + 3) * sizeof(float) + (size_t)3 * kMxKc * ns * sizeof(float);
   size_t large = (size_t)3 * kMxKc * max_n * sizeof(float);
   // the staged block row (or the tensor-core bands, aligned to 1024 bytes)
   if (max_n > small_max && large < sizeof(MxStage) + 1024) large = sizeof(MxStage) + 1024;
