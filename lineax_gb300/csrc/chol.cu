@@ -705,11 +705,20 @@ __device__ __forceinline__ void mx_rows_fma(float (&v)[W], float u, const float*
   }
 }
 
+// Rows [i_lo, i_hi) of D updated with the solved block [r0, r0+rn): row i's
+// coefficient of step t is u[i * si + t * st] (rows below the block in the
+// forward pass: u = U + r0*ld, si = 1, st = ld; rows above it in the backward
+// pass: u = U + r0, si = ld, st = 1).  One function, called (not inlined) at
+// the full chunk width by both passes, keeps the substitution's code small:
+// with two widths and a copy per pass the step took 1 % longer (instruction
+// fetch stalls of two CTAs in different phases), though padding vectors now
+// take their FMAs.
 template <int W>
-__device__ __forceinline__ void mx_solve_rows_below(const float* U, int ld, int n, int r0, int rn,
-                                                    float* D) {
+__device__ __noinline__ void mx_solve_rows(const float* u, int si, int st, int i_lo, int i_hi,
+                                          int r0, int rn, float* D) {
   static_assert(W % 4 == 0, "vectors go in groups of four");
-  for (int i = r0 + rn + threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = i_lo + threadIdx.x; i < i_hi; i += blockDim.x) {
+    const float* up = u + (int64_t)i * si;
     float v[W];
 #pragma unroll
     for (int c = 0; c < W; ++c) v[c] = D[i * kMxKc + c];
@@ -721,38 +730,12 @@ __device__ __forceinline__ void mx_solve_rows_below(const float* U, int ld, int 
       for (int t0 = 0; t0 < kMxNB; t0 += 16) {
         float uu[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) uu[k] = U[(r0 + t0 + k) * ld + i];
+        for (int k = 0; k < 16; ++k) uu[k] = up[(t0 + k) * st];
 #pragma unroll
         for (int k = 0; k < 16; ++k) mx_rows_fma<W>(v, uu[k], D + (r0 + t0 + k) * kMxKc);
       }
     } else {
-      for (int t = 0; t < rn; ++t) mx_rows_fma<W>(v, U[(r0 + t) * ld + i], D + (r0 + t) * kMxKc);
-    }
-#pragma unroll
-    for (int c = 0; c < W; ++c) D[i * kMxKc + c] = v[c];
-  }
-}
-
-template <int W>
-__device__ __forceinline__ void mx_solve_rows_above(const float* U, int ld, int n, int r0, int rn,
-                                                    float* D) {
-  static_assert(W % 4 == 0, "vectors go in groups of four");
-  for (int i = threadIdx.x; i < r0; i += blockDim.x) {
-    const float* rowp = U + i * ld + r0;
-    float v[W];
-#pragma unroll
-    for (int c = 0; c < W; ++c) v[c] = D[i * kMxKc + c];
-    if (rn == kMxNB) {
-#pragma unroll 1
-      for (int t0 = 0; t0 < kMxNB; t0 += 16) {
-        float uu[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) uu[k] = rowp[t0 + k];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) mx_rows_fma<W>(v, uu[k], D + (r0 + t0 + k) * kMxKc);
-      }
-    } else {
-      for (int t = 0; t < rn; ++t) mx_rows_fma<W>(v, rowp[t], D + (r0 + t) * kMxKc);
+      for (int t = 0; t < rn; ++t) mx_rows_fma<W>(v, up[t * st], D + (r0 + t) * kMxKc);
     }
 #pragma unroll
     for (int c = 0; c < W; ++c) D[i * kMxKc + c] = v[c];
@@ -782,10 +765,7 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
       if (lane < rn) D[(r0 + lane) * kMxKc + c] = v;
     }
     __syncthreads();
-    if (nc <= NC / 2)
-      mx_solve_rows_below<NC / 2>(U, ld, n, r0, rn, D);
-    else
-      mx_solve_rows_below<NC>(U, ld, n, r0, rn, D);
+    mx_solve_rows<NC>(U + (int64_t)r0 * ld, 1, ld, r0 + rn, n, r0, rn, D);
     __syncthreads();
   }
   for (int bi = nblk - 1; bi >= 0; --bi) {  // backward: U x = y
@@ -805,10 +785,7 @@ __device__ __noinline__ void mx_solve_t(const float* U, int ld, int n, int nc, f
       if (lane < rn) D[(r0 + lane) * kMxKc + c] = v;
     }
     __syncthreads();
-    if (nc <= NC / 2)
-      mx_solve_rows_above<NC / 2>(U, ld, n, r0, rn, D);
-    else
-      mx_solve_rows_above<NC>(U, ld, n, r0, rn, D);
+    mx_solve_rows<NC>(U + r0, ld, 1, 0, r0, r0, rn, D);
     __syncthreads();
   }
 }
