@@ -70,6 +70,50 @@ def test_request_larger_than_budget_is_rejected():
     assert [r.rid for r in s.rejected] == [0]
 
 
+class _HostOnlyServer(serve.SolveServer):
+    """The serving loop's host side (admission, worker threads, completion
+    bookkeeping) with jobs that touch no device: each job records whether its
+    operator's matrix is known when it runs and waits `delay[rid]` seconds."""
+
+    def __init__(self, delay, **kw):
+        super().__init__(torch.device("cuda", 0), mode="mixed", hbm_budget=1 << 34, **kw)
+        self.delay, self.seen = delay, {}
+
+    def _jobs(self, batch):
+        return [(self._fake, [r]) for r in batch]
+
+    def _fake(self, reqs):
+        import time
+
+        r = reqs[0]
+        time.sleep(self.delay.get(r.rid, 0.0))
+        self.seen[r.rid] = r.a is not None or r.op_id in self.registry
+        return [serve.Completion(r.rid, r.b, 0.0, "host", False, r.a is None)]
+
+    def _work(self, fn, reqs, t0):
+        import time
+
+        out = fn(reqs)
+        for c in out:
+            c.finished = time.perf_counter() - t0
+        return out
+
+
+def test_reuse_request_finds_its_matrix_when_it_runs_first():
+    # Request 0 defines operator 7 and is slow; request 1 reuses operator 7,
+    # arrives right after it and, on another worker, runs first.  The matrix
+    # must be known from the moment request 0 was sent.
+    reqs = [req(0, "lu", 600, op=7), req(1, "lu", 600, op=7, arrival=0.001, with_a=False),
+            req(2, "cholesky", 1200), req(3, "qr", 800, arrival=0.002)]
+    srv = _HostOnlyServer({0: 0.2}, streams=3)
+    out = srv.run(reqs, realtime=True)
+    assert [c.rid for c in out] == [0, 1, 2, 3]
+    assert all(srv.seen[r.rid] for r in reqs)
+    assert srv.seen and out[1].finished < out[0].finished   # the reuse really ran first
+    assert all(c.latency >= 0.0 for c in out)
+    assert srv.sched.inflight == 0                          # every job returned its footprint
+
+
 def test_synthetic_mix_shapes():
     reqs = serve.synthetic_requests(60, seed=1, nmax=600, rate=100.0)
     assert all(r.kind in serve.KINDS and 32 <= r.n <= 600 and 1 <= r.nrhs <= 16 for r in reqs)
