@@ -142,3 +142,10 @@ def test_serve_mix_backward_error_and_batch_independence(dev, mode):
                 alone.register(o.op_id, o.a)
         c = alone.run([serve.Request(r.rid, r.kind, r.b, r.op_id, r.a, 0.0)], realtime=False)[0]
         assert torch.equal(c.x, out[r.rid].x), (r.kind, r.n, c.route)
+
+
+def test_pipeline_flag_is_checked_once_per_request():
+    serve._check_pipeline(None)
+    serve._check_pipeline(torch.zeros(1, dtype=torch.int32))
+    with pytest.raises(RuntimeError, match="pipeline timed out"):
+        serve._check_pipeline(torch.ones(1, dtype=torch.int32))
