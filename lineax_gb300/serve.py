@@ -236,6 +236,13 @@ class Scheduler:
             self.resident.move_to_end(op_id)
             return hit[1]
 
+    def forget(self, op_id) -> None:
+        """Drop a resident operator (its factor turned out unusable)."""
+        with self.lock:
+            hit = self.resident.pop(op_id, None)
+            if hit is not None:
+                self.resident_total -= hit[0]
+
     def remember(self, op_id, nbytes: int, payload) -> None:
         with self.lock:
             if op_id in self.resident:
@@ -344,6 +351,17 @@ class SolveServer:
         ev.record(torch.cuda.current_stream(self.device))
         res.ready = ev
         self.sched.remember(op_id, resident_bytes(route, n), res)
+
+    def _check_or_forget(self, err, op_id) -> None:
+        """The request's pipeline flag (see _check_pipeline); on a timeout the
+        factor it published is dropped, so later requests on the operator
+        factor it again.  (A request that acquired it meanwhile still ends
+        correct: its refinement falls back to FP64 when it stalls.)"""
+        try:
+            _check_pipeline(err)
+        except RuntimeError:
+            self.sched.forget(op_id)
+            raise
 
     # -- execution ------------------------------------------------------------
 
@@ -485,7 +503,7 @@ class SolveServer:
                             inner_max_steps=5, restart=8, factor=res.factor,
                             inverse=res.inverse, split=res.split, precision=self.precision,
                             arith="auto", fallback=True)
-        _check_pipeline(err)
+        self._check_or_forget(err, req.op_id)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "lu_mixed", ir.fallback, reused)
 
@@ -509,7 +527,7 @@ class SolveServer:
                             inner_max_steps=5, restart=8, factor=res.factor,
                             inverse=res.inverse, split=res.split, precision=self.precision,
                             arith="auto", fallback=True)
-        _check_pipeline(err)
+        self._check_or_forget(err, req.op_id)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "chol_mixed", ir.fallback, reused)
 
@@ -526,7 +544,7 @@ class SolveServer:
         ir = mixed.gmres_ir(res.a, self._padded_rhs(req, n4), tol=self.tol, max_outer=20,
                             inner_max_steps=5, restart=8, split=res.split, qr=res.qr,
                             arith="auto", fallback=True)
-        _check_pipeline(err)
+        self._check_or_forget(err, req.op_id)
         x = ir.x[:, : req.n].contiguous()
         return Completion(req.rid, x, max(ir.berr), "qr_mixed", ir.fallback, reused)
 

@@ -149,3 +149,16 @@ def test_pipeline_flag_is_checked_once_per_request():
     serve._check_pipeline(torch.zeros(1, dtype=torch.int32))
     with pytest.raises(RuntimeError, match="pipeline timed out"):
         serve._check_pipeline(torch.ones(1, dtype=torch.int32))
+
+
+def test_resident_of_a_timed_out_factor_is_dropped():
+    srv = _HostOnlyServer({})
+    per = serve.resident_bytes("lu_mixed", 512)
+    srv.sched.remember(7, per, "factor")
+    srv._check_or_forget(torch.zeros(1, dtype=torch.int32), 7)     # flag clear: kept
+    assert srv.sched.lookup(7) == "factor"
+    with pytest.raises(RuntimeError, match="pipeline timed out"):
+        srv._check_or_forget(torch.ones(1, dtype=torch.int32), 7)
+    assert srv.sched.lookup(7) is None and srv.sched.resident_total == 0
+    srv.sched.forget(7)                                            # absent: no effect
+    assert srv.sched.resident_total == 0
